@@ -1,0 +1,153 @@
+"""Host-side mirror of the reference's suffix-sorter interface for the BWT path (adnaneben/kolmo
+src/algo/sais/sais.h:10-20), on the GPU engine.
+
+``bwt_aux`` / ``unbwt_aux`` / ``unbwt`` keep the reference's argument meaning and return codes (0, -1 bad arguments
+or indexes out of range, -2 out of memory); they return the output arrays alongside the code. ``fwd_batch`` and
+``inv_batch`` run many blocks in one device pass. ``Engine`` works on device-resident buffers (torch tensors) on a
+caller stream. Every call goes through the C ABI of ``libkgbwt.so``; nothing here computes a BWT on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+
+_DUMMY_A = np.zeros(1, np.int32)  # the caller's scratch: checked for NULL like the reference, never touched
+
+
+def n_samples(n: int, r: int) -> int:
+    return (n - 1) // r + 1 if n > 0 else 1
+
+
+def _u8(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.uint8)
+    return a if a.size else np.zeros(1, np.uint8)
+
+
+def bwt_aux(T, r: int):
+    """kolmo_sais_bwt_aux: returns (rc, U, I)."""
+    T = np.ascontiguousarray(T, dtype=np.uint8)
+    n = int(T.size)
+    Tb = _u8(T)
+    U = np.zeros(max(n, 1), np.uint8)
+    I = np.zeros(max(n_samples(n, r), 1), np.int32)
+    rc = native.lib().kolmo_sais_bwt_aux(Tb.ctypes.data, U.ctypes.data, _DUMMY_A.ctypes.data, n, r, I.ctypes.data, 1)
+    return int(rc), U[:n], I[: n_samples(n, r)]
+
+
+def unbwt_aux(U, r: int, I):
+    """kolmo_sais_unbwt_aux: returns (rc, T)."""
+    U = np.ascontiguousarray(U, dtype=np.uint8)
+    n = int(U.size)
+    Ub = _u8(U)
+    I = np.ascontiguousarray(I, dtype=np.int32)
+    out = np.zeros(max(n, 1), np.uint8)
+    rc = native.lib().kolmo_sais_unbwt_aux(Ub.ctypes.data, out.ctypes.data, _DUMMY_A.ctypes.data, n, r,
+                                           I.ctypes.data, 1)
+    return int(rc), out[:n]
+
+
+def unbwt(U, idx: int):
+    """kolmo_sais_unbwt: returns (rc, T)."""
+    U = np.ascontiguousarray(U, dtype=np.uint8)
+    n = int(U.size)
+    Ub = _u8(U)
+    out = np.zeros(max(n, 1), np.uint8)
+    rc = native.lib().kolmo_sais_unbwt(Ub.ctypes.data, out.ctypes.data, _DUMMY_A.ctypes.data, n, idx, 1)
+    return int(rc), out[:n]
+
+
+def fwd_batch(blocks, plain: bool = False):
+    """blocks: list of (T, r). Returns (rc, [(rc_i, U_i, I_i)])."""
+    keep, jobs = [], (native.FwdJob * max(len(blocks), 1))()
+    outs = []
+    for k, (T, r) in enumerate(blocks):
+        T = _u8(T) if np.asarray(T).size else np.zeros(1, np.uint8)
+        n = int(np.asarray(blocks[k][0]).size)
+        U = np.zeros(max(n, 1), np.uint8)
+        I = np.zeros(max(n_samples(n, r), 1), np.int32)
+        keep += [T, U, I]
+        jobs[k].T, jobs[k].U, jobs[k].n, jobs[k].r, jobs[k].I = T.ctypes.data, U.ctypes.data, n, r, I.ctypes.data
+        outs.append((U, I, n, r))
+    rc = native.lib().kgbwt_fwd_batch(jobs, len(blocks), native.PLAIN if plain else 0)
+    res = [(int(jobs[k].rc), U[:n], I[: n_samples(n, r)]) for k, (U, I, n, r) in enumerate(outs)]
+    return int(rc), res
+
+
+def inv_batch(blocks, plain: bool = False):
+    """blocks: list of (U, r, I). Returns (rc, [(rc_i, T_i)])."""
+    keep, jobs = [], (native.InvJob * max(len(blocks), 1))()
+    outs = []
+    for k, (U, r, I) in enumerate(blocks):
+        n = int(np.asarray(U).size)
+        Ub = _u8(U)
+        Ib = np.ascontiguousarray(I, dtype=np.int32)
+        out = np.zeros(max(n, 1), np.uint8)
+        keep += [Ub, Ib, out]
+        jobs[k].T, jobs[k].U, jobs[k].n, jobs[k].r, jobs[k].I = Ub.ctypes.data, out.ctypes.data, n, r, Ib.ctypes.data
+        outs.append((out, n))
+    rc = native.lib().kgbwt_inv_batch(jobs, len(blocks), native.PLAIN if plain else 0)
+    return int(rc), [(int(jobs[k].rc), out[:n]) for k, (out, n) in enumerate(outs)]
+
+
+class Engine:
+    """A device engine (one batch in flight). Buffers are torch CUDA tensors; calls enqueue on `stream`
+    (a torch.cuda.Stream or None for the current stream) and `wait()` synchronises and reports errors."""
+
+    def __init__(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0):
+        self.h = native.lib().kgbwt_engine_create()
+        if not self.h:
+            raise MemoryError("kgbwt_engine_create failed")
+        if tile_cap or tile_ctas or msd_ctas:
+            self.config(tile_cap, tile_ctas, msd_ctas)
+
+    def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0):
+        rc = native.lib().kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
+        if rc:
+            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas}")
+
+    def close(self):
+        if self.h:
+            native.lib().kgbwt_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _stream(stream):
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return ctypes.c_void_p(s.cuda_stream)
+
+    def fwd(self, dT, dL, dI, blocks, dSA=None, stream=None, plain: bool = False) -> int:
+        """blocks: sequence of (off, n, r, iout)."""
+        arr = (native.Block * len(blocks))(*[native.Block(*b) for b in blocks])
+        return int(native.lib().kgbwt_engine_fwd(self.h, dT.data_ptr(), dL.data_ptr(), dI.data_ptr(),
+                                                 dSA.data_ptr() if dSA is not None else None, arr, len(blocks),
+                                                 self._stream(stream), native.PLAIN if plain else 0))
+
+    def inv(self, dU, dOut, blocks, stream=None, plain: bool = False) -> int:
+        """blocks: sequence of (off, n, p0)."""
+        arr = (native.IBlock * len(blocks))(*[native.IBlock(b[0], b[1], b[2], 0) for b in blocks])
+        return int(native.lib().kgbwt_engine_inv(self.h, dU.data_ptr(), dOut.data_ptr(), arr, len(blocks),
+                                                 self._stream(stream), native.PLAIN if plain else 0))
+
+    def wait(self, nblocks: int = 0):
+        st = np.zeros(max(nblocks, 1), np.int32)
+        rc = native.lib().kgbwt_engine_wait(self.h, st.ctypes.data)
+        return int(rc), st[:nblocks]
+
+    def stats(self):
+        r, p, l = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+        native.lib().kgbwt_engine_stats(self.h, ctypes.byref(r), ctypes.byref(p), ctypes.byref(l))
+        return {"rounds": r.value, "passes": p.value, "launches": l.value}
+
+    def workspace_bytes(self) -> int:
+        return int(native.lib().kgbwt_engine_workspace_bytes(self.h))

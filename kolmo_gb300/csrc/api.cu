@@ -1,0 +1,335 @@
+// C ABI of the GB300 block-sorting engine: the reference's suffix-sorter entry points (drop-in), batch calls and
+// device-buffer engines. See include/kgbwt.h for the contract of every function.
+#include "kgbwt.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "fwd.cuh"
+#include "inv.cuh"
+
+namespace kgb {
+
+static thread_local char g_err[512];
+
+void record_error(const char *msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
+
+int record_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+    const char *f = strrchr(file, '/');
+    snprintf(g_err, sizeof g_err, "%s: %s (%s:%d)", what, cudaGetErrorString(e), f ? f + 1 : file, line);
+    return -2;
+}
+
+// Pinned host staging, grown on demand.
+struct Pinned {
+    u8 *p = nullptr;
+    size_t cap = 0;
+    int need(size_t bytes) {
+        if (bytes <= cap) return 0;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes + bytes / 4 + 4096;
+        KGB_CHECK(cudaMallocHost(&p, want));
+        cap = want;
+        return 0;
+    }
+    ~Pinned() { if (p) cudaFreeHost(p); }
+};
+
+}  // namespace kgb
+
+struct kgbwt_engine {
+    kgb::FwdEngine fwd;
+    kgb::InvEngine inv;
+    cudaStream_t last = nullptr;
+    int last_kind = 0;
+    std::vector<int> inv_status;
+    std::mutex mu;
+};
+
+namespace kgb {
+
+// The default context used by the drop-in and batch calls: one engine, one stream, pinned staging, one lock.
+struct Context {
+    std::mutex mu;
+    kgbwt_engine eng;
+    cudaStream_t stream = nullptr;
+    Pinned stage_L, stage_I;
+    bool ready = false;
+    int init() {
+        if (ready) return 0;
+        KGB_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        ready = true;
+        return 0;
+    }
+};
+static Context &ctx() {
+    static Context *c = new Context();  // never destroyed: callers may run at process exit
+    return *c;
+}
+
+static bool bad_r(int32_t r) { return r < 2 || (r & (r - 1)) != 0; }
+
+// KGBWT_PLAIN=1 in the environment makes the drop-in and batch calls use the plain path (debugging aid).
+static uint32_t env_flags() {
+    static int plain = -1;
+    if (plain < 0) { const char *e = getenv("KGBWT_PLAIN"); plain = e && e[0] == '1'; }
+    return plain ? KGBWT_PLAIN : 0u;
+}
+
+static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    if (int rc = C.init()) return rc;
+    std::vector<int> dev;
+    std::vector<u32> n, r;
+    for (int i = 0; i < count; i++) {
+        kgbwt_fwd_job &j = jobs[i];
+        if (!j.T || !j.U || !j.I || j.n < 0 || bad_r(j.r)) { j.rc = -1; continue; }
+        if (j.n <= 1) {
+            if (j.n == 1) j.U[0] = j.T[0];
+            j.I[0] = j.n;
+            j.rc = 0;
+            continue;
+        }
+        j.rc = 0;
+        dev.push_back(i);
+        n.push_back((u32)j.n);
+        r.push_back((u32)j.r);
+    }
+    if (dev.empty()) return 0;
+    FwdEngine &E = C.eng.fwd;
+    int rc = E.plan(n.data(), r.data(), (int)dev.size(), false);
+    if (rc) { for (int i : dev) jobs[i].rc = rc; return rc; }
+    cudaStream_t s = C.stream;
+    auto fail = [&](int code) { for (int i : dev) jobs[i].rc = code; return code; };
+    for (size_t k = 0; k < dev.size(); k++) {
+        if (cudaMemcpyAsync(E.text() + E.offsets()[k], jobs[dev[k]].T, n[k], cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
+    }
+    if (cudaMemsetAsync(E.text() + E.total(), 0, 64, s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__));
+    if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
+    const size_t lbytes = E.total() + dev.size();
+    if ((rc = C.stage_L.need(lbytes)) || (rc = C.stage_I.need((size_t)E.samples() * 4))) return fail(rc);
+    if (cudaMemcpyAsync(C.stage_L.p, E.lcol(), lbytes, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(C.stage_I.p, E.samples_dev(), (size_t)E.samples() * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(result)", __FILE__, __LINE__));
+    u32 err = 0;
+    if ((rc = E.error_flag(s, &err))) return fail(rc);
+    if (err) {
+        char m[96];
+        snprintf(m, sizeof m, "forward sort: device error bits 0x%x (internal error)", err);
+        record_error(m);
+        return fail(-2);
+    }
+    const u32 *I = reinterpret_cast<const u32 *>(C.stage_I.p);
+    for (size_t k = 0; k < dev.size(); k++) {
+        kgbwt_fwd_job &j = jobs[dev[k]];
+        const u8 *L = C.stage_L.p + E.offsets()[k] + k;
+        const u32 *Ib = I + E.iouts()[k];
+        const u32 ns = (u32)((j.n - 1) / j.r + 1);
+        const u32 p0 = Ib[0];
+        memcpy(j.U, L, p0);
+        memcpy(j.U + p0, L + p0 + 1, (size_t)j.n - p0);
+        for (u32 t = 0; t < ns; t++) j.I[t] = (int32_t)Ib[t];
+    }
+    return 0;
+}
+
+static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    if (int rc = C.init()) return rc;
+    std::vector<int> dev;
+    std::vector<u32> n, p0;
+    for (int i = 0; i < count; i++) {
+        kgbwt_inv_job &j = jobs[i];
+        if (!j.T || !j.U || !j.I || j.n < 0 || ((j.r != j.n) && bad_r(j.r))) { j.rc = -1; continue; }
+        if (j.n <= 1) {
+            if (j.I[0] != j.n) { j.rc = -1; continue; }
+            if (j.n == 1) j.U[0] = j.T[0];
+            j.rc = 0;
+            continue;
+        }
+        bool ok = true;
+        for (int32_t t = 0; t <= (j.n - 1) / j.r; t++)
+            if (j.I[t] <= 0 || j.I[t] > j.n) { ok = false; break; }
+        if (!ok) { j.rc = -1; continue; }
+        j.rc = 0;
+        dev.push_back(i);
+        n.push_back((u32)j.n);
+        p0.push_back((u32)j.I[0]);
+    }
+    if (dev.empty()) return 0;
+    InvEngine &E = C.eng.inv;
+    int rc = E.plan(n.data(), p0.data(), (int)dev.size());
+    auto fail = [&](int code) { for (int i : dev) jobs[i].rc = code; return code; };
+    if (rc) return fail(rc);
+    cudaStream_t s = C.stream;
+    for (size_t k = 0; k < dev.size(); k++)
+        if (cudaMemcpyAsync(E.input() + E.offsets()[k], jobs[dev[k]].T, n[k], cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(bwt)", __FILE__, __LINE__));
+    if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
+    if ((rc = C.stage_L.need(E.total()))) return fail(rc);
+    if (cudaMemcpyAsync(C.stage_L.p, E.output(), E.total(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
+    std::vector<int> st;
+    if ((rc = E.fetch_status(s, st))) return fail(rc);
+    int first = 0;
+    for (size_t k = 0; k < dev.size(); k++) {
+        kgbwt_inv_job &j = jobs[dev[k]];
+        if (st[k]) {
+            j.rc = -1;
+            if (!first) { first = -1; record_error("inverse BWT: not a valid BWT string for its primary index"); }
+            continue;
+        }
+        memcpy(j.U, C.stage_L.p + E.offsets()[k], (size_t)j.n);
+    }
+    return first;
+}
+
+}  // namespace kgb
+
+using namespace kgb;
+
+extern "C" {
+
+int32_t kolmo_sais_bwt_aux(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32_t r, int32_t *I,
+                           int32_t threads) {
+    (void)threads;
+    if (!T || !U || !A || n < 0 || bad_r(r) || !I) return -1;
+    kgbwt_fwd_job j = {T, U, n, r, I, 0};
+    int rc = fwd_batch_impl(&j, 1, env_flags());
+    return rc ? rc : j.rc;
+}
+
+int32_t kolmo_sais_unbwt_aux(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32_t r, const int32_t *I,
+                             int32_t threads) {
+    (void)threads;
+    if (!T || !U || !A || n < 0 || ((r != n) && bad_r(r)) || !I) return -1;
+    kgbwt_inv_job j = {T, U, n, r, I, 0};
+    int rc = inv_batch_impl(&j, 1, env_flags());
+    return rc ? rc : j.rc;
+}
+
+int32_t kolmo_sais_unbwt(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32_t i, int32_t threads) {
+    return kolmo_sais_unbwt_aux(T, U, A, n, n, &i, threads);
+}
+
+int32_t kgbwt_fwd_batch(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
+    if (!jobs || count < 0) return -1;
+    int rc = fwd_batch_impl(jobs, count, flags | env_flags());
+    if (rc) return rc;
+    for (int i = 0; i < count; i++) if (jobs[i].rc) return jobs[i].rc;
+    return 0;
+}
+
+int32_t kgbwt_inv_batch(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
+    if (!jobs || count < 0) return -1;
+    int rc = inv_batch_impl(jobs, count, flags | env_flags());
+    if (rc) return rc;
+    for (int i = 0; i < count; i++) if (jobs[i].rc) return jobs[i].rc;
+    return 0;
+}
+
+kgbwt_engine *kgbwt_engine_create(void) { return new (std::nothrow) kgbwt_engine(); }
+void kgbwt_engine_destroy(kgbwt_engine *e) { delete e; }
+
+int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas, int32_t msd_ctas) {
+    if (!e) return -1;
+    if (tile_cap && tile_cap != 4096 && tile_cap != 8192) return -1;
+    if (tile_ctas < 0 || tile_ctas > 8 || msd_ctas < 0 || msd_ctas > 16) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    if (tile_cap && tile_cap != e->fwd.cfg.tile_cap) {
+        // a different tile capacity changes list capacities: drop the workspace (it is rebuilt on the next call)
+        e->fwd.~FwdEngine();
+        new (&e->fwd) FwdEngine();
+        e->fwd.cfg.tile_cap = tile_cap;
+    }
+    if (tile_ctas) e->fwd.cfg.tile_ctas = tile_ctas;
+    if (msd_ctas) e->fwd.cfg.msd_ctas = msd_ctas;
+    return 0;
+}
+
+int32_t kgbwt_engine_fwd(kgbwt_engine *e, const uint8_t *dT, uint8_t *dL, int32_t *dI, int32_t *dSA,
+                         const kgbwt_block *blocks, int32_t count, void *stream, uint32_t flags) {
+    if (!e || !dT || !dL || !dI || !blocks || count <= 0) return -1;
+    if (((uintptr_t)dT & 7) != 0) { record_error("text buffer must be 8-byte aligned"); return -1; }
+    std::lock_guard<std::mutex> lock(e->mu);
+    std::vector<u32> off(count), n(count), r(count), io(count);
+    for (int b = 0; b < count; b++) {
+        if (blocks[b].n < 2 || bad_r((int32_t)blocks[b].r) || blocks[b].n > 0x7FFFFFFFu) return -1;
+        off[b] = blocks[b].off; n[b] = blocks[b].n; r[b] = blocks[b].r; io[b] = blocks[b].iout;
+    }
+    int rc = e->fwd.plan_external(off.data(), n.data(), r.data(), io.data(), count, const_cast<uint8_t *>(dT), dL,
+                                  reinterpret_cast<u32 *>(dI), reinterpret_cast<u32 *>(dSA));
+    if (rc) return rc;
+    e->last = (cudaStream_t)stream;
+    e->last_kind = 1;
+    return e->fwd.run((cudaStream_t)stream, !(flags & KGBWT_PLAIN));
+}
+
+int32_t kgbwt_engine_inv(kgbwt_engine *e, const uint8_t *dU, uint8_t *dOut, const kgbwt_iblock *blocks,
+                         int32_t count, void *stream, uint32_t flags) {
+    if (!e || !dU || !dOut || !blocks || count <= 0) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    std::vector<u32> off(count), n(count), p0(count);
+    for (int b = 0; b < count; b++) {
+        if (blocks[b].n < 2 || blocks[b].p0 < 1 || blocks[b].p0 > blocks[b].n || blocks[b].n > 0x7FFFFFFFu) return -1;
+        off[b] = blocks[b].off; n[b] = blocks[b].n; p0[b] = blocks[b].p0;
+    }
+    int rc = e->inv.plan_external(off.data(), n.data(), p0.data(), count, const_cast<uint8_t *>(dU), dOut);
+    if (rc) return rc;
+    e->last = (cudaStream_t)stream;
+    e->last_kind = 2;
+    return e->inv.run((cudaStream_t)stream, !(flags & KGBWT_PLAIN));
+}
+
+int32_t kgbwt_engine_wait(kgbwt_engine *e, int32_t *status) {
+    if (!e) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    if (e->last_kind == 1) {
+        u32 err = 0;
+        if (int rc = e->fwd.error_flag(e->last, &err)) return rc;
+        if (err) { record_error("forward sort: round limit exceeded (internal error)"); return -2; }
+        return 0;
+    }
+    if (e->last_kind == 2) {
+        std::vector<int> st;
+        if (int rc = e->inv.fetch_status(e->last, st)) return rc;
+        int first = 0;
+        for (size_t b = 0; b < st.size(); b++) {
+            int v = st[b] ? -1 : 0;
+            if (status) status[b] = v;
+            if (v && !first) first = v;
+        }
+        return first;
+    }
+    return 0;
+}
+
+int32_t kgbwt_engine_stats(kgbwt_engine *e, int32_t *rounds, int32_t *passes, int64_t *launches) {
+    if (!e) return -1;
+    if (e->last_kind == 2) {
+        if (rounds) *rounds = 0;
+        if (passes) *passes = e->inv.stats.jumps;
+        if (launches) *launches = e->inv.stats.launches;
+        return 0;
+    }
+    if (rounds) *rounds = e->fwd.stats.rounds;
+    if (passes) *passes = e->fwd.stats.passes;
+    if (launches) *launches = e->fwd.stats.launches;
+    return 0;
+}
+
+uint64_t kgbwt_engine_workspace_bytes(kgbwt_engine *e) { return e ? e->fwd.workspace_bytes() + e->inv.workspace_bytes() : 0; }
+
+const char *kgbwt_last_error(void) { return g_err; }
+int32_t kgbwt_version(void) { return 100; }
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// Shared device helpers for the block-sorting kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace kgb {
+
+typedef uint8_t u8;
+typedef uint16_t u16;
+typedef uint32_t u32;
+typedef unsigned long long u64;
+
+// Error plumbing: every CUDA call on the host goes through KGB_CHECK, which records the failure and makes the
+// enclosing function return the C-ABI code (-2 for resources and device errors).
+int record_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+void record_error(const char *msg);
+#define KGB_CHECK(x)                                                                         \
+    do {                                                                                     \
+        cudaError_t e__ = (x);                                                               \
+        if (e__ != cudaSuccess) return ::kgb::record_cuda_error(e__, #x, __FILE__, __LINE__); \
+    } while (0)
+
+// Bounds guards of the checked build (-DKGB_CHECKED): `KGB_GUARD(cond, err, bit) stmt;` runs stmt only when cond
+// holds and otherwise sets `bit` in the device error word *err. In the normal build it is just `stmt;`.
+#ifdef KGB_CHECKED
+#define KGB_GUARD(cond, errp, bit) \
+    if (!(cond)) {                 \
+        atomicOr((errp), (bit));   \
+    } else
+#define KGB_OK(cond, errp, bit) ((cond) ? true : (atomicOr((errp), (bit)), false))
+#else
+#define KGB_GUARD(cond, errp, bit)
+#define KGB_OK(cond, errp, bit) true
+#endif
+
+__device__ __forceinline__ u32 lanemask_lt() {
+    u32 m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ u32 lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ u32 warp_id() { return threadIdx.x >> 5; }
+
+__device__ __forceinline__ u32 warp_incl_sum(u32 v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        u32 t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane_id() >= (u32)o) v += t;
+    }
+    return v;
+}
+__device__ __forceinline__ u32 warp_incl_max(u32 v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        u32 t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane_id() >= (u32)o) v = max(v, t);
+    }
+    return v;
+}
+__device__ __forceinline__ u32 warp_sum(u32 v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide exclusive sum over NT threads (NT multiple of 32, <= 1024). `ws` needs NT/32 + 1 words of shared
+// memory. Returns the thread's exclusive prefix; *total receives the block sum. Contains __syncthreads().
+template <int NT>
+__device__ __forceinline__ u32 block_excl_sum(u32 v, u32 *ws, u32 *total) {
+    constexpr int W = NT / 32;
+    u32 inc = warp_incl_sum(v);
+    if (lane_id() == 31) ws[warp_id()] = inc;
+    __syncthreads();
+    if (warp_id() == 0) {
+        u32 x = lane_id() < (u32)W ? ws[lane_id()] : 0u;
+        u32 xi = warp_incl_sum(x);
+        if (lane_id() < (u32)W) ws[lane_id()] = xi - x;
+        if (lane_id() == (u32)W - 1) ws[W] = xi;
+    }
+    __syncthreads();
+    u32 r = ws[warp_id()] + inc - v;
+    if (total) *total = ws[W];
+    __syncthreads();
+    return r;
+}
+
+// Block-wide inclusive max-scan over NT threads; `ws` needs NT/32 words. Contains __syncthreads().
+template <int NT>
+__device__ __forceinline__ u32 block_incl_max(u32 v, u32 *ws) {
+    constexpr int W = NT / 32;
+    u32 inc = warp_incl_max(v);
+    if (lane_id() == 31) ws[warp_id()] = inc;
+    __syncthreads();
+    if (warp_id() == 0) {
+        u32 x = lane_id() < (u32)W ? ws[lane_id()] : 0u;
+        u32 xi = warp_incl_max(x);
+        if (lane_id() < (u32)W) ws[lane_id()] = xi;
+    }
+    __syncthreads();
+    u32 before = warp_id() ? ws[warp_id() - 1] : 0u;
+    __syncthreads();
+    return max(before, inc);
+}
+
+// 8 bytes of T starting at i as a big-endian word (T[i] most significant). T must have 16 readable bytes past
+// every position read and an 8-byte aligned base.
+__device__ __forceinline__ u64 load_be64(const u8 *__restrict__ T, u64 i) {
+    const u64 *p = reinterpret_cast<const u64 *>(T + (i & ~7ull));
+    u64 a = __ldg(p), b = __ldg(p + 1);
+    u32 s = (u32)(i & 7) * 8;
+    u64 w = s ? (a >> s) | (b << (64 - s)) : a;
+    u32 lo = (u32)w, hi = (u32)(w >> 32);
+    return ((u64)__byte_perm(lo, 0, 0x0123) << 32) | (u64)__byte_perm(hi, 0, 0x0123);
+}
+
+}  // namespace kgb

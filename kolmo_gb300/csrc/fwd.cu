@@ -1,0 +1,1203 @@
+// Forward BWT on the GPU: prefix-doubling suffix sorting over a batch of independent blocks (sm_103a).
+//
+// Algorithm (Manber-Myers prefix doubling, as restated for GPUs by the reference's Metal sorter,
+// src/arch/metal/sa_metal.m:1-13 and src/arch/metal/sa.metal:178-256 of adnaneben/kolmo):
+//   round 0   group all suffixes by their first 8 bytes (zero padded past the block end);
+//   round j   h = 8 * 2^(j-1) characters are sorted; every suffix i still in a group of two or more ("active") is
+//             re-sorted inside its group by rank(i + h), where past the end of the block the key is below every
+//             rank and decreases with i (a shorter suffix sorts first: the reference's implicit sentinel);
+//   a suffix alone in its group is final: its rank is its suffix-array position.
+// The rank of a group is the suffix-array position of its first member (sa.metal:209-217).
+//
+// GB300 formulation. There is no global sort per round. Groups are segments of an element list and are refined
+// in place of a sort:
+//   * groups of up to SMAX elements are packed into tiles of TILE elements and sorted inside shared memory (one
+//     CTA per tile, block-wide LSD radix over only the key bytes that vary in the tile); the same kernel gathers
+//     the keys, splits the groups, writes ranks and the L column of finished suffixes, and appends the surviving
+//     groups to the next round's list. One kernel, one read of each active suffix per round.
+//   * larger groups go through most-significant-digit bucket passes (histogram, per-group scan, scatter) until
+//     their buckets fit a tile or hold one key value.
+// Ranks are double-buffered: a round gathers from isa[rpar] and writes isa[rpar ^ 1], so no round reads a rank
+// that the same round refined. Suffixes finished in a round are copied into the other buffer during the next.
+// The L column is written as suffixes finish (row p + 1 = T[SA[p] - 1], the reference's BWT convention
+// sais.c:12043-12049), so no suffix array pass is needed. A device control block drives every loop, so the whole
+// sort is one CUDA graph with conditional while-nodes (no host synchronisation), or, for the plain path, one
+// kernel launch per step with a host read of the control block after every pass.
+#include "fwd.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+namespace kgb {
+
+constexpr int TPB = 256;
+constexpr int TSM = 2048;  // elements per tile of the bucket passes
+constexpr int IPM = TSM / TPB;
+constexpr u32 DEPTH_PREFIX = 8, DEPTH_RANK = 4;
+
+enum : u8 { C_NONE = 0, C_KS = 1, C_KO = 2, C_LN = 3, C_ONE = 4 };
+
+struct FwdArgs {
+    Ctl *ctl;
+    const u8 *T;
+    const BlockInfo *blk;
+    u32 *isa[2];
+    u8 *L;
+    u32 *SA;
+    u32 *I;
+    ListView lists[NLISTS];
+    u32 *hist, *cursor, *bhead, *orand;
+    u8 *dest;
+    u32 B;
+    u32 smax;
+    unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
+    // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
+    u64 cap_n, cap_segs, cap_segl, cap_tms, cap_tml;
+};
+
+// device error bits
+enum : u32 { E_ROUNDS = 1, E_PASSES = 2, E_TILE = 4, E_LIST = 8, E_SEG = 16, E_TMAP = 32, E_RANK = 64, E_HIST = 128 };
+
+__device__ __forceinline__ u32 seg_blk(u32 bd) { return bd & 0xFFFFFFu; }
+__device__ __forceinline__ u32 seg_depth(u32 bd) { return bd >> 24; }
+
+// Depth of the first bucket pass of a rank-round group from the OR/AND of its keys: the byte of the highest
+// varying bit (3 when all keys are equal, which then finishes the group in one pass).
+__device__ __forceinline__ u32 depth_from_vary(u32 orv, u32 andv) {
+    u32 vary = orv ^ andv;
+    if (!vary) return DEPTH_RANK - 1;
+    u32 msb = 31 - __clz(vary);
+    return (31 - msb) >> 3;
+}
+
+// Byte d of the zero-padded 8-byte prefix of suffix i of a block ending at `end`.
+__device__ __forceinline__ u32 prefix_byte(const u8 *__restrict__ T, u32 i, u32 d, u64 end) {
+    return (u64)i + d < end ? (u32)__ldg(T + i + d) : 0u;
+}
+
+// Rank-round key of suffix i (block ending at `end`), h characters sorted: rank(i + h) + h, or, past the end,
+// end - 1 - i (below every shifted rank, decreasing with i).
+__device__ __forceinline__ u32 rank_key(const u32 *__restrict__ isa, u32 i, u32 h, u64 end) {
+    u32 d = (u32)(end - i);
+    return h < d ? __ldg(isa + i + h) + h : d - 1;
+}
+
+// The final state of a suffix: rank = suffix-array position p (block-local), L column row p + 1 = T[i - 1]
+// (the sentinel row's byte value is never read), optional suffix array, and its index in the resolved list.
+__device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, ListView res,
+                                        u32 ridx) {
+    BlockInfo B = a.blk[b];
+    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
+        return;
+    isa_nxt[id] = p;
+    a.L[(u64)B.off + b + p + 1] = id == B.off ? 0 : __ldg(a.T + id - 1);
+    if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
+    res.eid[ridx] = id;
+}
+
+// ------------------------------------------------------------------------------------------------ tile sorter
+// Tile t of a small-group list covers every segment whose start lies in [t * TS, (t + 1) * TS) (TS = TILE / 2 =
+// SMAX, so a tile holds at most TILE elements). tmap[t] = index of the first such segment; the producers of a
+// list write it (a segment covering position t * TS writes tmap[t]: its own index if it starts there, else the next).
+
+template <int TILE>
+struct TileSmem {
+    static constexpr int TS = TILE / 2;
+    u64 klo[TILE];
+    u32 val[TILE];
+    u16 khi[TILE];
+    u16 wcnt[TPB / 32][256];
+    u32 lstart[TS + 1];
+    u32 lhead[TS];
+    u32 lblk[TS];
+    u32 ws[TPB / 32 + 1];
+    u32 ws2[TPB / 32 + 1];
+    u64 red[4][TPB / 32];
+    u32 bases[4];
+};
+
+__device__ __forceinline__ void write_tmap_small(const FwdArgs &a, u32 *tmap, u32 ts, u32 start, u32 len, u32 sidx) {
+    u32 t = (start + ts - 1) / ts;
+    if ((u64)t * ts < (u64)start + len) {
+        KGB_GUARD(t < a.cap_tms, &a.ctl->err, E_TMAP) tmap[t] = (u64)t * ts == start ? sidx : sidx + 1;
+    }
+}
+
+template <bool PREFIX, bool KEYED, int TILE>
+__global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
+    constexpr int TS = TILE / 2, IPT = TILE / TPB, WS = 32 * IPT, NW = TPB / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem<TILE> &S = *reinterpret_cast<TileSmem<TILE> *>(smem_raw);
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h;
+    const u32 lin = KEYED ? L_KS : L_S0 + rpar;
+    const ListView in = a.lists[lin];
+    const ListView out = a.lists[L_S0 + (rpar ^ 1)];
+    const ListView res = a.lists[L_R0 + rpar];
+    const u64 c = ctl->cnt[lin];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segs) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 ntiles = (u32)(((u64)nelem + TS - 1) / TS);
+    const u32 *isa_cur = a.isa[rpar];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 lane = lane_id(), warp = warp_id(), tid = threadIdx.x;
+
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const u32 sa_ = in.tmap[t];
+        const u32 sb_ = t + 1 < ntiles ? in.tmap[t + 1] : nseg;
+        if (sa_ > nseg || sb_ > nseg) {
+            if (threadIdx.x == 0) atomicOr(&a.ctl->err, E_TMAP);
+            continue;
+        }
+        if (sa_ >= sb_) continue;
+        const u32 nsegs = sb_ - sa_;
+        const u32 E0 = in.seg[sa_].start;
+        const u32 E1 = sb_ < nseg ? in.seg[sb_].start : nelem;
+        const u32 cnt = E1 - E0;
+        if (nsegs > TS || E1 < E0 || cnt > TILE || E1 > nelem) {  // broken list invariant: report, never overrun
+            if (tid == 0) atomicOr(&a.ctl->err, E_TILE);
+            continue;
+        }
+        for (u32 j = tid; j < nsegs; j += TPB) {
+            Seg g = in.seg[sa_ + j];
+            S.lstart[j] = g.start - E0;
+            S.lhead[j] = g.head;
+            S.lblk[j] = seg_blk(g.bd);
+        }
+        if (tid == 0) S.lstart[nsegs] = cnt;
+        __syncthreads();
+
+        // ---- load: warp-striped arrangement, x = warp * WS + j * 32 + lane
+        u64 k[IPT];
+        u32 hi[IPT], v[IPT];
+        u64 orl = 0, andl = ~0ull;
+        u32 orh = 0, andh = ~0u;
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const u32 x = warp * WS + j * 32 + lane;
+            if (x < cnt) {
+                const u32 id = in.eid[E0 + x];
+                u32 lo = 0, hh = nsegs - 1;
+                while (lo < hh) {
+                    u32 mid = (lo + hh + 1) >> 1;
+                    if (S.lstart[mid] <= x) lo = mid; else hh = mid - 1;
+                }
+                u64 key;
+                if (PREFIX) {
+                    const BlockInfo B = a.blk[S.lblk[lo]];
+                    const u64 end = (u64)B.off + B.n;
+                    key = load_be64(a.T, id);
+                    const u64 rem = end - id;
+                    if (rem < 8) key &= ~0ull << (8 * (8 - rem));
+                } else if (KEYED) {
+                    key = in.ekey[E0 + x];
+                } else {
+                    const BlockInfo B = a.blk[S.lblk[lo]];
+                    key = rank_key(isa_cur, id, h, (u64)B.off + B.n);
+                }
+                k[j] = key;
+                hi[j] = lo;
+                v[j] = id;
+                orl |= key; andl &= key; orh |= lo; andh &= lo;
+            } else {
+                k[j] = ~0ull;
+                hi[j] = 0xFFFFu;
+                v[j] = 0;
+            }
+        }
+        // ---- which key bytes vary inside the tile
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            orl |= __shfl_xor_sync(0xffffffffu, orl, o);
+            andl &= __shfl_xor_sync(0xffffffffu, andl, o);
+            orh |= __shfl_xor_sync(0xffffffffu, orh, o);
+            andh &= __shfl_xor_sync(0xffffffffu, andh, o);
+        }
+        if (lane == 0) { S.red[0][warp] = orl; S.red[1][warp] = andl; S.red[2][warp] = orh; S.red[3][warp] = andh; }
+        __syncthreads();
+        orl = 0; andl = ~0ull; orh = 0; andh = ~0u;
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            orl |= S.red[0][w]; andl &= S.red[1][w]; orh |= (u32)S.red[2][w]; andh &= (u32)S.red[3][w];
+        }
+        const u64 vary_lo = orl ^ andl;
+        const u32 vary_hi = (orh ^ andh) & 0xFFFFu;
+
+        // ---- LSD radix over the varying bytes: 8 bytes of the key, then 2 bytes of the segment index
+        bool in_smem = false;
+        for (int digit = 0; digit < 10; digit++) {
+            const bool lo_part = digit < 8;
+            const u32 sh = lo_part ? 8 * digit : 8 * (digit - 8);
+            if (lo_part ? !((vary_lo >> sh) & 0xFF) : !((vary_hi >> sh) & 0xFF)) continue;
+            for (int i = tid; i < NW * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
+            __syncthreads();
+            u32 dg[IPT], rk[IPT];
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 d = lo_part ? (u32)(k[j] >> sh) & 0xFF : (hi[j] >> sh) & 0xFF;
+                dg[j] = d;
+                const u32 peers = __match_any_sync(0xffffffffu, d);
+                const u32 before = S.wcnt[warp][d];
+                rk[j] = before + __popc(peers & lanemask_lt());
+                __syncwarp();
+                if ((__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
+                __syncwarp();
+            }
+            __syncthreads();
+            {   // digit-major exclusive scan: thread tid owns digit tid
+                u32 tot = 0;
+#pragma unroll
+                for (int w = 0; w < NW; w++) tot += S.wcnt[w][tid];
+                u32 run = block_excl_sum<TPB>(tot, S.ws, nullptr);
+#pragma unroll
+                for (int w = 0; w < NW; w++) { u32 cc = S.wcnt[w][tid]; S.wcnt[w][tid] = (u16)run; run += cc; }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 dst = S.wcnt[warp][dg[j]] + rk[j];
+                S.klo[dst] = k[j];
+                S.khi[dst] = (u16)hi[j];
+                S.val[dst] = v[j];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                k[j] = S.klo[x]; hi[j] = S.khi[x]; v[j] = S.val[x];
+            }
+            in_smem = true;
+            __syncthreads();
+        }
+        if (!in_smem) {
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                S.klo[x] = k[j]; S.khi[x] = (u16)hi[j]; S.val[x] = v[j];
+            }
+            __syncthreads();
+        }
+
+        // ---- split groups: blocked arrangement x = tid * IPT + j
+        u32 st[IPT], en[IPT];
+        u32 gl = 0, ns = 0, ng = 0;
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const u32 x = tid * IPT + j;
+            st[j] = en[j] = 0;
+            if (x < cnt) {
+                const u32 sj = S.khi[x];
+                const u64 kx = S.klo[x];
+                st[j] = x == S.lstart[sj] || kx != S.klo[x - 1];
+                en[j] = x + 1 == S.lstart[sj + 1] || kx != S.klo[x + 1];
+                if (st[j]) gl = x;
+                const u32 surv = !(st[j] && en[j]);
+                ns += surv;
+                ng += surv && st[j];
+            }
+        }
+        // group first member: inclusive max-scan of group starts (gl = last start in this thread, or 0)
+        const u32 incl = block_incl_max<TPB>(gl, S.ws);
+        __syncthreads();
+        u32 carry;
+        {
+            // exclusive max = inclusive max of the previous thread
+            __shared__ u32 prevmax[TPB];
+            prevmax[tid] = incl;
+            __syncthreads();
+            carry = tid ? prevmax[tid - 1] : 0u;
+            __syncthreads();
+        }
+        u32 tot_pack = 0;
+        const u32 pre = block_excl_sum<TPB>(ns | (ng << 16), S.ws, &tot_pack);
+        const u32 tot_s = tot_pack & 0xFFFFu, tot_g = tot_pack >> 16;
+        if (tid == 0) {
+            const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)tot_g << 32) | tot_s);
+            S.bases[0] = (u32)o;
+            S.bases[1] = (u32)(o >> 32);
+            S.bases[2] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)(cnt - tot_s));
+        }
+        __syncthreads();
+        const u32 ebase = S.bases[0], sbase = S.bases[1], rbase = S.bases[2];
+        u32 es = pre & 0xFFFFu, gs = pre >> 16;
+        u32 gfirst = carry;
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const u32 x = tid * IPT + j;
+            if (x >= cnt) break;
+            if (st[j]) gfirst = x;
+            const u32 sj = S.khi[x], id = S.val[x];
+            const u32 s0 = S.lstart[sj];
+            if (st[j] && en[j]) {
+                resolve(a, isa_nxt, id, S.lhead[sj] + (x - s0), S.lblk[sj], res, rbase + (x - es));
+            } else {
+                const u32 head = S.lhead[sj] + (gfirst - s0);
+                KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+                KGB_GUARD(ebase + es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + es] = id;
+                if (st[j]) gs++;
+                if (en[j]) {
+                    const u32 len = x - gfirst + 1, sidx = sbase + gs - 1, start = ebase + es + 1 - len;
+                    Seg g;
+                    g.start = start; g.len = len; g.head = head; g.bd = S.lblk[sj];
+                    KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
+                    write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                }
+                es++;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ bucket passes
+// Work lists of large groups are tiled by TSM elements; every group is longer than TSM, so a tile meets at most
+// two. tmap[t] = the group containing element t * TSM.
+
+struct MsdTile {
+    u32 s0, s1, bound, d0, d1;
+    Seg g0, g1;
+};
+
+template <bool PREFIX>
+__device__ __forceinline__ void msd_tile_info(const FwdArgs &a, const ListView &in, u32 nseg, u32 t, bool first,
+                                              MsdTile &m) {
+    m.s0 = in.tmap[t];
+    if (m.s0 >= nseg) {  // broken tile map: report and use a valid index (the round result is discarded)
+        atomicOr(&a.ctl->err, E_TMAP);
+        m.s0 = 0;
+    }
+    m.g0 = in.seg[m.s0];
+    m.bound = m.g0.start + m.g0.len;
+    m.s1 = m.s0 + 1 < nseg ? m.s0 + 1 : m.s0;
+    m.g1 = in.seg[m.s1];
+    if (!PREFIX && first) {
+        m.d0 = depth_from_vary(a.orand[2 * m.s0], a.orand[2 * m.s0 + 1]);
+        m.d1 = depth_from_vary(a.orand[2 * m.s1], a.orand[2 * m.s1 + 1]);
+    } else {
+        m.d0 = seg_depth(m.g0.bd);
+        m.d1 = seg_depth(m.g1.bd);
+    }
+}
+
+template <bool PREFIX>
+__device__ __forceinline__ u32 msd_digit(const FwdArgs &a, const ListView &in, u32 x, u32 id, const Seg &g, u32 d,
+                                         u32 *key) {
+    if (PREFIX) {
+        const BlockInfo B = a.blk[seg_blk(g.bd)];
+        return prefix_byte(a.T, id, d, (u64)B.off + B.n);
+    }
+    *key = in.ekey[x];
+    return (*key >> (24 - 8 * d)) & 0xFF;
+}
+
+// Rank rounds, first pass: gather the keys of the large groups and the OR/AND of each group's keys.
+__global__ void __launch_bounds__(TPB) k_keygen(FwdArgs a) {
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h;
+    const ListView in = a.lists[L_L0 + rpar];
+    const u64 c = ctl->cnt[L_L0 + rpar];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segl) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 ntiles = (nelem + TSM - 1) / TSM;
+    const u32 *isa = a.isa[rpar];
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const u32 s0 = in.tmap[t];
+        if (s0 >= nseg) { if (threadIdx.x == 0) atomicOr(&a.ctl->err, E_TMAP); continue; }
+        const Seg g0 = in.seg[s0];
+        const u32 bound = g0.start + g0.len, s1 = s0 + 1 < nseg ? s0 + 1 : s0;
+        const Seg g1 = in.seg[s1];
+        const BlockInfo B0 = a.blk[seg_blk(g0.bd)], B1 = a.blk[seg_blk(g1.bd)];
+        u32 or0 = 0, and0 = ~0u, or1 = 0, and1 = ~0u;
+#pragma unroll
+        for (int j = 0; j < IPM; j++) {
+            const u32 x = t * TSM + j * TPB + threadIdx.x;
+            if (x < nelem) {
+                const bool sel = x >= bound;
+                const BlockInfo &B = sel ? B1 : B0;
+                const u32 id = in.eid[x];
+                const u32 key = rank_key(isa, id, h, (u64)B.off + B.n);
+                in.ekey[x] = key;
+                if (sel) { or1 |= key; and1 &= key; } else { or0 |= key; and0 &= key; }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            or0 |= __shfl_xor_sync(0xffffffffu, or0, o);
+            and0 &= __shfl_xor_sync(0xffffffffu, and0, o);
+            or1 |= __shfl_xor_sync(0xffffffffu, or1, o);
+            and1 &= __shfl_xor_sync(0xffffffffu, and1, o);
+        }
+        if (lane_id() == 0) {
+            if (or0 || and0 != ~0u) { atomicOr(&a.orand[2 * s0], or0); atomicAnd(&a.orand[2 * s0 + 1], and0); }
+            if (s1 != s0 && (or1 || and1 != ~0u)) { atomicOr(&a.orand[2 * s1], or1); atomicAnd(&a.orand[2 * s1 + 1], and1); }
+        }
+    }
+}
+
+__device__ __forceinline__ const ListView &msd_in(const FwdArgs &a, u32 rpar, u32 pass, u32 *lid) {
+    *lid = pass == 0 ? L_L0 + rpar : L_K0 + ((pass - 1) & 1);
+    return a.lists[*lid];
+}
+
+template <bool PREFIX>
+__global__ void __launch_bounds__(TPB) k_msd_hist(FwdArgs a) {
+    __shared__ u32 hs[2][256];
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, pass = ctl->pass;
+    u32 lid;
+    const ListView in = msd_in(a, rpar, pass, &lid);
+    const u64 c = ctl->cnt[lid];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segl) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 ntiles = (nelem + TSM - 1) / TSM;
+    const u32 lane = lane_id();
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (int i = threadIdx.x; i < 512; i += TPB) (&hs[0][0])[i] = 0;
+        MsdTile m;
+        msd_tile_info<PREFIX>(a, in, nseg, t, pass == 0, m);
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < IPM; j++) {
+            const u32 x = t * TSM + j * TPB + threadIdx.x;
+            const bool valid = x < nelem;
+            u32 kk = 0xFFFFFFFFu;
+            if (valid) {
+                const bool sel = x >= m.bound;
+                u32 key;
+                const u32 d = msd_digit<PREFIX>(a, in, x, in.eid[x], sel ? m.g1 : m.g0, sel ? m.d1 : m.d0, &key);
+                kk = ((u32)sel << 8) | d;
+            }
+            const u32 peers = __match_any_sync(0xffffffffu, kk);
+            if (valid && (__ffs(peers) - 1) == (int)lane) atomicAdd(&(&hs[0][0])[kk], __popc(peers));
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 512; i += TPB) {
+            const u32 cc = (&hs[0][0])[i];
+            if (cc) {
+                const u32 sx = i < 256 ? m.s0 : m.s1;
+                KGB_GUARD(sx < a.cap_segl, &a.ctl->err, E_HIST) atomicAdd(&a.hist[(u64)sx * 256 + (i & 255)], cc);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+struct ScanSmem {
+    u32 ws[TPB / 32 + 1];
+    u32 base_e[5], base_s[5];
+    u32 nb_off[TPB];
+    u32 t0[TPB];
+    u32 sidx[TPB];
+    u8 cls[TPB];
+};
+
+// One CTA per group of the pass: bucket sizes -> class, destination and descriptors of every bucket.
+template <bool PREFIX>
+__global__ void __launch_bounds__(TPB) k_msd_scan(FwdArgs a) {
+    __shared__ ScanSmem S;
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, pass = ctl->pass;
+    u32 lid;
+    const ListView in = msd_in(a, rpar, pass, &lid);
+    const u32 nseg = min((u32)(ctl->cnt[lid] >> 32), (u32)a.cap_segl);
+    const u32 lko = L_K0 + (pass & 1), lln = L_L0 + (rpar ^ 1);
+    const u32 tid = threadIdx.x;
+    for (u32 s = blockIdx.x; s < nseg; s += gridDim.x) {
+        if (s >= a.cap_segl) { if (tid == 0) atomicOr(&a.ctl->err, E_HIST); break; }
+        const Seg g = in.seg[s];
+        u32 d;
+        if (!PREFIX && pass == 0) {
+            d = depth_from_vary(a.orand[2 * s], a.orand[2 * s + 1]);
+        } else {
+            d = seg_depth(g.bd);
+        }
+        const u64 hrow = (u64)s * 256;
+        const u32 cc = a.hist[hrow + tid];
+        a.hist[hrow + tid] = 0;
+        const u32 excl = block_excl_sum<TPB>(cc, S.ws, nullptr);
+        const u32 nd = d + 1, maxd = PREFIX ? DEPTH_PREFIX : DEPTH_RANK;
+        u8 cls = cc == 0 ? C_NONE : cc == 1 ? C_ONE : cc <= a.smax ? C_KS : nd >= maxd ? C_LN : C_KO;
+        // element and segment counts per class (singletons need only a resolved-list slot)
+        u32 e_ks = cls == C_KS ? cc : 0, e_ko = cls == C_KO ? cc : 0, e_ln = cls == C_LN ? cc : 0;
+        u32 tks, tko, tln, tone;
+        const u32 x_ks = block_excl_sum<TPB>(e_ks, S.ws, &tks);
+        const u32 x_ko = block_excl_sum<TPB>(e_ko, S.ws, &tko);
+        const u32 x_ln = block_excl_sum<TPB>(e_ln, S.ws, &tln);
+        const u32 spack = (cls == C_KS) | ((u32)(cls == C_KO) << 10) | ((u32)(cls == C_LN) << 20);
+        u32 tsp;
+        const u32 x_sp = block_excl_sum<TPB>(spack, S.ws, &tsp);
+        const u32 x_one = block_excl_sum<TPB>(cls == C_ONE, S.ws, &tone);
+        if (tid == 0) {
+            if (tks) { u64 o = atomicAdd(&a.ctl->cnt[L_KS], ((u64)(tsp & 1023) << 32) | tks); S.base_e[C_KS] = (u32)o; S.base_s[C_KS] = (u32)(o >> 32); }
+            if (tko) { u64 o = atomicAdd(&a.ctl->cnt[lko], ((u64)((tsp >> 10) & 1023) << 32) | tko); S.base_e[C_KO] = (u32)o; S.base_s[C_KO] = (u32)(o >> 32); }
+            if (tln) { u64 o = atomicAdd(&a.ctl->cnt[lln], ((u64)((tsp >> 20) & 1023) << 32) | tln); S.base_e[C_LN] = (u32)o; S.base_s[C_LN] = (u32)(o >> 32); }
+            if (tone) { S.base_e[C_ONE] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)tone); }
+        }
+        __syncthreads();
+        const u32 head = g.head + excl, blk = seg_blk(g.bd);
+        u32 nb = 0, t0 = 0, sidx = 0;
+        if (cls == C_ONE) {
+            a.cursor[hrow + tid] = S.base_e[C_ONE] + x_one;  // slot in the resolved list
+        } else if (cls != C_NONE) {
+            u32 start;
+            ListView o;
+            u32 bd = blk;
+            if (cls == C_KS) { start = S.base_e[C_KS] + x_ks; sidx = S.base_s[C_KS] + (x_sp & 1023); o = a.lists[L_KS]; }
+            else if (cls == C_KO) { start = S.base_e[C_KO] + x_ko; sidx = S.base_s[C_KO] + ((x_sp >> 10) & 1023); o = a.lists[lko]; bd |= nd << 24; }
+            else { start = S.base_e[C_LN] + x_ln; sidx = S.base_s[C_LN] + ((x_sp >> 20) & 1023); o = a.lists[lln]; }
+            Seg ng;
+            ng.start = start; ng.len = cc; ng.head = head; ng.bd = bd;
+            KGB_GUARD(sidx < (cls == C_KS ? a.cap_segs : a.cap_segl) && (u64)start + cc <= a.cap_n, &a.ctl->err, E_SEG)
+            o.seg[sidx] = ng;
+            a.cursor[hrow + tid] = start;
+            if (cls == C_KS) {
+                write_tmap_small(a, o.tmap, a.smax, start, cc, sidx);
+            } else {
+                t0 = (start + TSM - 1) / TSM;
+                const u32 t1 = (u32)(((u64)start + cc - 1) / TSM);
+                nb = t1 >= t0 ? t1 - t0 + 1 : 0;
+            }
+        }
+        a.bhead[hrow + tid] = head;
+        a.dest[hrow + tid] = cls;
+        if (!PREFIX && pass == 0 && tid == 0) {  // the scatter reads the digit from the descriptor
+            a.orand[2 * s] = 0;
+            a.orand[2 * s + 1] = ~0u;
+            in.seg[s].bd = blk | (d << 24);
+        }
+        // tile-map entries of the large buckets, spread over the CTA
+        u32 nbt;
+        const u32 nbx = block_excl_sum<TPB>(nb, S.ws, &nbt);
+        S.nb_off[tid] = nbx; S.t0[tid] = t0; S.sidx[tid] = sidx; S.cls[tid] = cls;
+        __syncthreads();
+        for (u32 q = tid; q < nbt; q += TPB) {
+            u32 lo = 0, hh = TPB - 1;  // last bucket with nb_off <= q and a nonzero count
+            while (lo < hh) {
+                u32 mid = (lo + hh + 1) >> 1;
+                if (S.nb_off[mid] <= q) lo = mid; else hh = mid - 1;
+            }
+            // the last bucket whose range starts at or before q owns q (later buckets start past it)
+            ListView o = a.lists[S.cls[lo] == C_KO ? lko : lln];
+            const u32 ti = S.t0[lo] + (q - S.nb_off[lo]);
+            KGB_GUARD(ti < a.cap_tml, &a.ctl->err, E_TMAP) o.tmap[ti] = S.sidx[lo];
+        }
+        __syncthreads();
+    }
+}
+
+template <bool PREFIX>
+__global__ void __launch_bounds__(TPB) k_msd_scatter(FwdArgs a) {
+    __shared__ u32 cnt[2][256];
+    __shared__ u32 base[2][256];
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, pass = ctl->pass;
+    u32 lid;
+    const ListView in = msd_in(a, rpar, pass, &lid);
+    const u64 c = ctl->cnt[lid];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segl) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 ntiles = (nelem + TSM - 1) / TSM;
+    const ListView ks = a.lists[L_KS], ko = a.lists[L_K0 + (pass & 1)], ln = a.lists[L_L0 + (rpar ^ 1)];
+    const ListView res = a.lists[L_R0 + rpar];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 lane = lane_id();
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (int i = threadIdx.x; i < 512; i += TPB) (&cnt[0][0])[i] = 0;
+        MsdTile m;
+        msd_tile_info<PREFIX>(a, in, nseg, t, false, m);  // digits come from the descriptors the scan updated
+        __syncthreads();
+        u32 kk[IPM], slot[IPM], ids[IPM], keys[IPM];
+#pragma unroll
+        for (int j = 0; j < IPM; j++) {
+            const u32 x = t * TSM + j * TPB + threadIdx.x;
+            const bool valid = x < nelem;
+            kk[j] = 0xFFFFFFFFu;
+            if (valid) {
+                const bool sel = x >= m.bound;
+                ids[j] = in.eid[x];
+                const u32 d = msd_digit<PREFIX>(a, in, x, ids[j], sel ? m.g1 : m.g0, sel ? m.d1 : m.d0, &keys[j]);
+                kk[j] = ((u32)sel << 8) | d;
+            }
+            const u32 peers = __match_any_sync(0xffffffffu, kk[j]);
+            const int leader = __ffs(peers) - 1;
+            u32 old = 0;
+            if (valid && leader == (int)lane) old = atomicAdd(&(&cnt[0][0])[kk[j]], __popc(peers));
+            old = __shfl_sync(0xffffffffu, old, leader);
+            slot[j] = old + __popc(peers & lanemask_lt());
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 512; i += TPB) {
+            const u32 cc = (&cnt[0][0])[i];
+            if (cc) {
+                const u64 row = (u64)(i < 256 ? m.s0 : m.s1) * 256 + (i & 255);
+                (&base[0][0])[i] = a.dest[row] == C_ONE ? a.cursor[row] : atomicAdd(&a.cursor[row], cc);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < IPM; j++) {
+            if (kk[j] == 0xFFFFFFFFu) continue;
+            const u32 sel = kk[j] >> 8, d = kk[j] & 255;
+            const u64 row = (u64)(sel ? m.s1 : m.s0) * 256 + d;
+            const u8 cls = a.dest[row];
+            const u32 pos = (&base[0][0])[kk[j]] + slot[j];
+            const u32 id = ids[j];
+            if (!KGB_OK(pos < a.cap_n && id < a.cap_n, &a.ctl->err, E_LIST)) continue;
+            if (cls == C_KS) {
+                ks.eid[pos] = id;
+                if (!PREFIX) ks.ekey[pos] = keys[j];
+            } else if (cls == C_KO) {
+                ko.eid[pos] = id;
+                if (!PREFIX) ko.ekey[pos] = keys[j];
+            } else if (cls == C_LN) {
+                ln.eid[pos] = id;
+                isa_nxt[id] = a.bhead[row];
+            } else {  // C_ONE
+                resolve(a, isa_nxt, id, a.bhead[row], seg_blk((sel ? m.g1 : m.g0).bd), res, pos);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// The suffixes resolved in the previous round: copy their final rank into this round's write buffer.
+__global__ void __launch_bounds__(TPB) k_fixup(FwdArgs a) {
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar;
+    const ListView r = a.lists[L_R0 + (rpar ^ 1)];
+    const u32 n = min((u32)ctl->cnt[L_R0 + (rpar ^ 1)], (u32)a.cap_n);
+    const u32 *cur = a.isa[rpar];
+    u32 *nxt = a.isa[rpar ^ 1];
+    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
+        const u32 id = r.eid[i];
+        nxt[id] = cur[id];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ control
+__device__ __forceinline__ void set_cond(unsigned long long h, u32 v) {
+    if (h) cudaGraphSetConditional((cudaGraphConditionalHandle)h, v);
+}
+__device__ __forceinline__ u32 elems(const Ctl *c, u32 l) { return (u32)c->cnt[l]; }
+
+__global__ void k_ctl_msd_begin(FwdArgs a) {
+    Ctl *c = a.ctl;
+    c->pass = 0;
+    c->cnt[L_K0] = 0;
+    set_cond(a.hcond, elems(c, L_L0 + c->rpar) > 0);
+}
+__global__ void k_ctl_msd_next(FwdArgs a) {
+    Ctl *c = a.ctl;
+    const u32 p = c->pass;
+    const u32 produced = L_K0 + (p & 1);
+    if (p == 0) c->cnt[L_L0 + c->rpar] = 0; else c->cnt[L_K0 + ((p - 1) & 1)] = 0;
+    c->pass = p + 1;
+    const u32 more = elems(c, produced) > 0;
+    if (p + 1 > 2 * DEPTH_PREFIX + 2) { c->err |= 2; set_cond(a.hcond, 0); return; }
+    set_cond(a.hcond, more);
+}
+__global__ void k_ctl_round_end(FwdArgs a) {
+    Ctl *c = a.ctl;
+    const u32 rp = c->rpar;
+    const u32 active = elems(c, L_S0 + (rp ^ 1)) + elems(c, L_L0 + (rp ^ 1));
+    c->cnt[L_S0 + rp] = 0;
+    c->cnt[L_L0 + rp] = 0;
+    c->cnt[L_KS] = 0;
+    c->cnt[L_K0] = 0;
+    c->cnt[L_K1] = 0;
+    c->cnt[L_R0 + (rp ^ 1)] = 0;
+    c->rpar = rp ^ 1;
+    c->round += 1;
+    c->h = c->round == 1 ? 8 : c->h * 2;
+    c->pass = 0;
+    u32 cont = active > 0;
+    if (cont && c->round > c->maxrounds) { c->err |= 1; cont = 0; }
+    c->done = !cont;
+    set_cond(a.hcond, cont);
+}
+
+// Sampled indexes: I[k] = 1 + rank of suffix k * r (I[0] is the primary index).
+__global__ void k_samples(FwdArgs a) {
+    const u32 *isa = a.isa[a.ctl->rpar];
+    for (u32 b = blockIdx.x; b < a.B; b += gridDim.x) {
+        const BlockInfo B = a.blk[b];
+        const u32 ns = (B.n - 1) / B.r + 1;
+        for (u32 k = threadIdx.x; k < ns; k += blockDim.x) a.I[B.iout + k] = isa[B.off + k * B.r] + 1;
+    }
+}
+
+// Element lists of round 0: blocks up to SMAX bytes are single small groups, longer blocks single large ones.
+// The L column's row 0 (the sentinel rotation) holds the block's last byte.
+__global__ void k_init(FwdArgs a, const u32 *__restrict__ blk_list_start, const u8 *__restrict__ blk_is_large) {
+    const u32 B = a.B;
+    for (u32 b = blockIdx.x; b < B; b += gridDim.x) {
+        const BlockInfo bi = a.blk[b];
+        const ListView l = a.lists[blk_is_large[b] ? L_L0 : L_S0];
+        const u32 st = blk_list_start[b];
+        for (u32 j = threadIdx.x; j < bi.n; j += blockDim.x) l.eid[st + j] = bi.off + j;
+        if (threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ host engine
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+FwdEngine::FwdEngine() {
+    for (auto &l : lists) l = ListView{nullptr, nullptr, nullptr, nullptr};
+}
+FwdEngine::~FwdEngine() { free_all(); }
+
+void FwdEngine::free_all() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+    if (pool) cudaFree(pool);
+    if (h_ctl) cudaFreeHost(h_ctl);
+    pool = nullptr;
+    h_ctl = nullptr;
+    pool_bytes = 0;
+    Ncap = 0;
+    Bcap = Icap = 0;
+}
+
+int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
+    if (ncap <= Ncap && bcap <= Bcap && icap <= Icap && (!want_sa || sa_cap)) return 0;
+    ncap = std::max<u64>(ncap, Ncap);
+    bcap = std::max<u32>(bcap, Bcap);
+    icap = std::max<u32>(icap, Icap);
+    want_sa = want_sa || sa_cap;
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (pool) { cudaFree(pool); pool = nullptr; }
+    const u64 n = ncap;
+    const u32 smax = (u32)cfg.tile_cap / 2;
+    const u64 nseg_small = n / 2 + bcap + 8;
+    const u64 nseg_large = n / smax + bcap + 8;
+    const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
+    struct Item { void **p; size_t bytes; };
+    std::vector<Item> items;
+    auto add = [&](void **p, size_t bytes) { items.push_back({p, align_up(std::max<size_t>(bytes, 16), 256)}); };
+    add((void **)&own_T, n + 64);
+    add((void **)&own_L, n + bcap + 64);
+    add((void **)&own_I, (size_t)icap * 4 + 16);
+    own_SA = nullptr;
+    if (want_sa) add((void **)&own_SA, n * 4);
+    add((void **)&d_isa[0], n * 4);
+    add((void **)&d_isa[1], n * 4);
+    add((void **)&d_blk, (size_t)bcap * sizeof(BlockInfo));
+    for (int l = 0; l < NLISTS; l++) {
+        lists[l] = ListView{nullptr, nullptr, nullptr, nullptr};
+        add((void **)&lists[l].eid, n * 4);
+        const bool small = l == L_S0 || l == L_S1 || l == L_KS;
+        const bool res = l == L_R0 || l == L_R1;
+        if (!res && l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
+        if (!res) {
+            add((void **)&lists[l].seg, (small ? nseg_small : nseg_large) * sizeof(Seg));
+            add((void **)&lists[l].tmap, (small ? ntm_small : ntm_large) * 4);
+        }
+    }
+    add((void **)&d_hist, nseg_large * 256 * 4);
+    add((void **)&d_cursor, nseg_large * 256 * 4);
+    add((void **)&d_bhead, nseg_large * 256 * 4);
+    add((void **)&d_dest, nseg_large * 256);
+    add((void **)&d_orand, nseg_large * 8);
+    add((void **)&d_ctl, sizeof(Ctl));
+    size_t total = 0;
+    for (auto &it : items) total += it.bytes;
+    cudaError_t e = cudaMalloc(&pool, total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        pool = nullptr;
+        Ncap = 0;
+        return record_cuda_error(e, "cudaMalloc(forward workspace)", __FILE__, __LINE__);
+    }
+    pool_bytes = total;
+    size_t off = 0;
+    for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
+    KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
+    // orand rows start as (or = 0, and = ~0)
+    {
+        std::vector<u32> init(2 * nseg_large);
+        for (size_t i = 0; i < nseg_large; i++) { init[2 * i] = 0; init[2 * i + 1] = ~0u; }
+        KGB_CHECK(cudaMemcpy(d_orand, init.data(), init.size() * 4, cudaMemcpyHostToDevice));
+    }
+    if (!h_ctl) KGB_CHECK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
+    Ncap = ncap;
+    Bcap = bcap;
+    Icap = icap;
+    sa_cap = want_sa;
+    cap_segs = nseg_small; cap_segl = nseg_large; cap_tms = ntm_small; cap_tml = ntm_large;
+    return 0;
+}
+
+void FwdEngine::set_caps(FwdArgs &a) const {
+    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_tms = cap_tms; a.cap_tml = cap_tml;
+}
+
+int FwdEngine::plan(const u32 *n, const u32 *r, int count, bool want_sa) {
+    if (count <= 0) return -1;
+    h_off.resize(count); h_n.resize(count); h_r.resize(count); h_iout.resize(count);
+    u64 off = 0, io = 0;
+    maxn = 0;
+    for (int b = 0; b < count; b++) {
+        if (n[b] < 2 || r[b] < 2) return -1;
+        h_off[b] = (u32)off; h_n[b] = n[b]; h_r[b] = r[b]; h_iout[b] = (u32)io;
+        off += n[b];
+        io += (n[b] - 1) / r[b] + 1;
+        maxn = std::max(maxn, n[b]);
+        if (off > 0xFFFF0000ull || io > 0xFFFF0000ull) return -1;
+    }
+    N = off; B = (u32)count; nI = (u32)io;
+    ext = false;
+    want_sa_run = want_sa;
+    int rc = grow(N, B, nI, want_sa);
+    if (rc) return rc;
+    d_T = own_T; d_L = own_L; d_I = own_I; d_SA = want_sa ? own_SA : nullptr;
+    return 0;
+}
+
+int FwdEngine::plan_external(const u32 *off, const u32 *n, const u32 *r, const u32 *iout, int count, u8 *dT, u8 *dL,
+                             u32 *dI, u32 *dSA) {
+    if (count <= 0) return -1;
+    h_off.assign(off, off + count); h_n.assign(n, n + count); h_r.assign(r, r + count); h_iout.assign(iout, iout + count);
+    u64 end = 0, io = 0;
+    maxn = 0;
+    for (int b = 0; b < count; b++) {
+        if (n[b] < 2 || r[b] < 2) return -1;
+        end = std::max<u64>(end, (u64)off[b] + n[b]);
+        io = std::max<u64>(io, (u64)iout[b] + (n[b] - 1) / r[b] + 1);
+        maxn = std::max(maxn, n[b]);
+    }
+    if (end > 0xFFFF0000ull) return -1;
+    N = end; B = (u32)count; nI = (u32)io;
+    ext = true;
+    want_sa_run = dSA != nullptr;
+    int rc = grow(N, B, 0, false);
+    if (rc) return rc;
+    d_T = dT; d_L = dL; d_I = dI; d_SA = dSA;
+    return 0;
+}
+
+static int ceil_log2(u64 x) { int k = 0; while ((1ull << k) < x) k++; return k; }
+
+int FwdEngine::setup_round0(cudaStream_t s) {
+    // block table, round-0 lists and their tile maps are laid out on the host (B entries, small)
+    const u32 smax = (u32)cfg.tile_cap / 2;
+    std::vector<BlockInfo> bi(B);
+    std::vector<u32> lstart(B);
+    std::vector<u8> large(B);
+    std::vector<Seg> seg_s, seg_l;
+    std::vector<u32> tm_s, tm_l;
+    u64 es = 0, el = 0;
+    for (u32 b = 0; b < B; b++) {
+        bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b]};
+        large[b] = h_n[b] > smax;
+        Seg g;
+        g.len = h_n[b]; g.head = 0; g.bd = b;
+        if (large[b]) {
+            g.start = (u32)el; lstart[b] = (u32)el;
+            for (u64 t = (el + TSM - 1) / TSM; t * TSM < el + h_n[b]; t++) { if (tm_l.size() <= t) tm_l.resize(t + 1); tm_l[t] = (u32)seg_l.size(); }
+            seg_l.push_back(g);
+            el += h_n[b];
+        } else {
+            g.start = (u32)es; lstart[b] = (u32)es;
+            u64 t = (es + smax - 1) / smax;
+            if (t * smax < es + h_n[b]) { if (tm_s.size() <= t) tm_s.resize(t + 1); tm_s[t] = (u32)seg_s.size() + (t * smax == es ? 0 : 1); }
+            seg_s.push_back(g);
+            es += h_n[b];
+        }
+    }
+    // staging: the small vectors go through one pinned buffer
+    Ctl c;
+    memset(&c, 0, sizeof(c));
+    c.cnt[L_S0] = ((u64)seg_s.size() << 32) | es;
+    c.cnt[L_L0] = ((u64)seg_l.size() << 32) | el;
+    c.maxrounds = (u32)ceil_log2(maxn) + 3;
+    KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
+    if (!seg_s.empty()) {
+        KGB_CHECK(cudaMemcpyAsync(lists[L_S0].seg, seg_s.data(), seg_s.size() * sizeof(Seg), cudaMemcpyHostToDevice, s));
+        if (!tm_s.empty()) KGB_CHECK(cudaMemcpyAsync(lists[L_S0].tmap, tm_s.data(), tm_s.size() * 4, cudaMemcpyHostToDevice, s));
+    }
+    if (!seg_l.empty()) {
+        KGB_CHECK(cudaMemcpyAsync(lists[L_L0].seg, seg_l.data(), seg_l.size() * sizeof(Seg), cudaMemcpyHostToDevice, s));
+        KGB_CHECK(cudaMemcpyAsync(lists[L_L0].tmap, tm_l.data(), tm_l.size() * 4, cudaMemcpyHostToDevice, s));
+    }
+    *h_ctl = c;
+    KGB_CHECK(cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    // per-block list starts and classes: stored behind the block table in the histogram rows, which are zero
+    // outside a bucket pass and are restored to zero by k_init's caller below
+    u32 *d_lstart = d_cursor;
+    u8 *d_large = d_dest;
+    KGB_CHECK(cudaMemcpyAsync(d_lstart, lstart.data(), B * 4, cudaMemcpyHostToDevice, s));
+    KGB_CHECK(cudaMemcpyAsync(d_large, large.data(), B, cudaMemcpyHostToDevice, s));
+    // these host vectors must outlive the async copies
+    KGB_CHECK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const isa[2], u8 *L, u32 *SA, u32 *I,
+                         const ListView *lists, u32 *hist, u32 *cursor, u32 *bhead, u32 *orand, u8 *dest, u32 B,
+                         u32 smax) {
+    FwdArgs a;
+    memset(&a, 0, sizeof(a));
+    a.ctl = ctl; a.T = T; a.blk = blk; a.isa[0] = isa[0]; a.isa[1] = isa[1]; a.L = L; a.SA = SA; a.I = I;
+    for (int l = 0; l < NLISTS; l++) a.lists[l] = lists[l];
+    a.hist = hist; a.cursor = cursor; a.bhead = bhead; a.orand = orand; a.dest = dest; a.B = B; a.smax = smax;
+    a.hcond = 0;
+    return a;
+}
+
+template <int TILE>
+static int tile_smem() { return (int)sizeof(TileSmem<TILE>); }
+
+struct Launcher {
+    cudaStream_t s;
+    int grid_tile, grid_msd, grid_scan, tile_cap;
+    long long *launches;
+    template <typename K, typename... Args>
+    cudaError_t go(K kern, int grid, int block, size_t smem, Args... args) {
+        kern<<<grid, block, smem, s>>>(args...);
+        (*launches)++;
+        return cudaGetLastError();
+    }
+};
+
+static bool g_attr_done[4] = {false, false, false, false};
+static int set_tile_attrs(int tile) {
+    int idx = tile == 8192 ? 1 : 0;
+    if (g_attr_done[idx]) return 0;
+    if (tile == 4096) {
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
+    } else {
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
+    }
+    g_attr_done[idx] = true;
+    return 0;
+}
+
+// Kernel sequences shared by the plain and graph paths.
+static cudaError_t enq_tile(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
+    if (L.tile_cap == 4096) {
+        const size_t sm = tile_smem<4096>();
+        if (prefix) return keyed ? L.go(k_tile_sort<true, true, 4096>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<true, false, 4096>, L.grid_tile, TPB, sm, a);
+        return keyed ? L.go(k_tile_sort<false, true, 4096>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<false, false, 4096>, L.grid_tile, TPB, sm, a);
+    }
+    const size_t sm = tile_smem<8192>();
+    if (prefix) return keyed ? L.go(k_tile_sort<true, true, 8192>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<true, false, 8192>, L.grid_tile, TPB, sm, a);
+    return keyed ? L.go(k_tile_sort<false, true, 8192>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<false, false, 8192>, L.grid_tile, TPB, sm, a);
+}
+static cudaError_t enq_msd_pass(Launcher &L, const FwdArgs &a, bool prefix) {
+    cudaError_t e;
+    if (prefix) {
+        if ((e = L.go(k_msd_hist<true>, L.grid_msd, TPB, 0, a))) return e;
+        if ((e = L.go(k_msd_scan<true>, L.grid_scan, TPB, 0, a))) return e;
+        return L.go(k_msd_scatter<true>, L.grid_msd, TPB, 0, a);
+    }
+    if ((e = L.go(k_msd_hist<false>, L.grid_msd, TPB, 0, a))) return e;
+    if ((e = L.go(k_msd_scan<false>, L.grid_scan, TPB, 0, a))) return e;
+    return L.go(k_msd_scatter<false>, L.grid_msd, TPB, 0, a);
+}
+
+static int report_err(u32 bits) {
+    char m[96];
+    snprintf(m, sizeof m, "forward sort: device error bits 0x%x (internal error)", bits);
+    record_error(m);
+    return -2;
+}
+
+int FwdEngine::run_plain(cudaStream_t s) {
+    const u32 smax = (u32)cfg.tile_cap / 2;
+    FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
+                          B, smax);
+    set_caps(a);
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &stats.launches};
+    KGB_CHECK(L.go(k_init, std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
+    auto read_ctl = [&]() -> int {
+        KGB_CHECK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+        KGB_CHECK(cudaStreamSynchronize(s));
+        return 0;
+    };
+    for (int round = 0;; round++) {
+        const bool prefix = round == 0;
+        if (!prefix) KGB_CHECK(L.go(k_fixup, grid_msd, TPB, 0, a));
+        if (!prefix) KGB_CHECK(L.go(k_keygen, grid_msd, TPB, 0, a));
+        KGB_CHECK(L.go(k_ctl_msd_begin, 1, 1, 0, a));
+        if (int rc = read_ctl()) return rc;
+        u32 more = (u32)h_ctl->cnt[L_L0 + h_ctl->rpar] > 0;
+        while (more) {
+            KGB_CHECK(enq_msd_pass(L, a, prefix));
+            KGB_CHECK(L.go(k_ctl_msd_next, 1, 1, 0, a));
+            stats.passes++;
+            if (int rc = read_ctl()) return rc;
+            if (h_ctl->err) return report_err(h_ctl->err);
+            more = (u32)h_ctl->cnt[L_K0 + ((h_ctl->pass - 1) & 1)] > 0;
+        }
+        KGB_CHECK(enq_tile(L, a, prefix, false));
+        KGB_CHECK(enq_tile(L, a, prefix, true));
+        KGB_CHECK(L.go(k_ctl_round_end, 1, 1, 0, a));
+        stats.rounds++;
+        if (int rc = read_ctl()) return rc;
+        if (h_ctl->err) return report_err(h_ctl->err);
+        if (h_ctl->done) break;
+    }
+    KGB_CHECK(L.go(k_samples, std::min<u32>(B, 1024u), 128, 0, a));
+    return 0;
+}
+
+// Graph: init -> round 0 -> while (active) { rank round } -> samples, where a round is
+//   fixup, keygen, msd_begin -> while (pass input non-empty) { hist, scan, scatter, msd_next } -> tiles, round_end.
+// Round 0 (prefix keys) is laid out once before the loop, the rank round is the loop body; the loops close with
+// conditional while-nodes whose handles the 1-thread control kernels set.
+typedef std::vector<cudaGraphNode_t> Deps;
+
+// Captures the kernels enqueued by fn into graph g after the nodes in deps; returns the new leaves in deps.
+template <typename F>
+static int capture_into(cudaStream_t s, cudaGraph_t g, Deps &deps, F fn) {
+    KGB_CHECK(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                            cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = fn();
+    const cudaGraphNode_t *d = nullptr;
+    size_t nd = 0;
+    cudaStreamCaptureStatus st;
+    cudaError_t e2 = cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &d, nullptr, &nd);
+    Deps leaves(d, d + (e2 == cudaSuccess ? nd : 0));
+    cudaGraph_t out = g;
+    cudaError_t e3 = cudaStreamEndCapture(s, &out);
+    KGB_CHECK(e);
+    KGB_CHECK(e2);
+    KGB_CHECK(e3);
+    deps = leaves;
+    return 0;
+}
+
+static int add_while(cudaGraph_t g, Deps &deps, cudaGraphConditionalHandle h, cudaGraph_t *body) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    KGB_CHECK(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &cp));
+    *body = cp.conditional.phGraph_out[0];
+    deps.assign(1, node);
+    return 0;
+}
+
+// One round (prefix or rank) into graph g after deps; hmsd closes its bucket-pass loop, hround is set by its end.
+static int add_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L, const FwdArgs &a, bool prefix,
+                     cudaGraphConditionalHandle hmsd, cudaGraphConditionalHandle hround) {
+    FwdArgs am = a, ar = a;
+    am.hcond = (unsigned long long)hmsd;
+    ar.hcond = (unsigned long long)hround;
+    if (int rc = capture_into(s, g, deps, [&]() -> cudaError_t {
+            cudaError_t e;
+            if (!prefix) {
+                if ((e = L.go(k_fixup, L.grid_msd, TPB, 0, a))) return e;
+                if ((e = L.go(k_keygen, L.grid_msd, TPB, 0, a))) return e;
+            }
+            return L.go(k_ctl_msd_begin, 1, 1, 0, am);
+        }))
+        return rc;
+    cudaGraph_t mbody;
+    if (int rc = add_while(g, deps, hmsd, &mbody)) return rc;
+    Deps md;
+    if (int rc = capture_into(s, mbody, md, [&]() -> cudaError_t {
+            cudaError_t e = enq_msd_pass(L, a, prefix);
+            if (e) return e;
+            return L.go(k_ctl_msd_next, 1, 1, 0, am);
+        }))
+        return rc;
+    return capture_into(s, g, deps, [&]() -> cudaError_t {
+        cudaError_t e;
+        if ((e = enq_tile(L, a, prefix, false))) return e;
+        if ((e = enq_tile(L, a, prefix, true))) return e;
+        return L.go(k_ctl_round_end, 1, 1, 0, ar);
+    });
+}
+
+int FwdEngine::build_graph(cudaStream_t s) {
+    const u32 smax = (u32)cfg.tile_cap / 2;
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    KGB_CHECK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle hround, hmsd0, hmsd;
+    KGB_CHECK(cudaGraphConditionalHandleCreate(&hround, graph, 0, cudaGraphCondAssignDefault));
+    KGB_CHECK(cudaGraphConditionalHandleCreate(&hmsd0, graph, 0, cudaGraphCondAssignDefault));
+    KGB_CHECK(cudaGraphConditionalHandleCreate(&hmsd, graph, 0, cudaGraphCondAssignDefault));
+    FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
+                          B, smax);
+    set_caps(a);
+    long long dummy = 0;
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &dummy};
+    Deps deps;
+    if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
+            return L.go(k_init, (int)std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
+        }))
+        return rc;
+    if (int rc = add_round(s, graph, deps, L, a, true, hmsd0, hround)) return rc;
+    cudaGraph_t rbody;
+    if (int rc = add_while(graph, deps, hround, &rbody)) return rc;
+    Deps rd;
+    if (int rc = add_round(s, rbody, rd, L, a, false, hmsd, hround)) return rc;
+    if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
+            return L.go(k_samples, (int)std::min<u32>(B, 1024u), 128, 0, a);
+        }))
+        return rc;
+    KGB_CHECK(cudaGraphInstantiate(&gexec, graph, 0));
+    return 0;
+}
+
+int FwdEngine::run(cudaStream_t s, bool use_graph) {
+    stats = FwdStats{};
+    if (!sm_count) {
+        int dev;
+        KGB_CHECK(cudaGetDevice(&dev));
+        KGB_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+    }
+    if (int rc = set_tile_attrs(cfg.tile_cap)) return rc;
+    grid_tile = sm_count * cfg.tile_ctas;
+    grid_msd = sm_count * cfg.msd_ctas;
+    grid_scan = sm_count * 4;
+    // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan
+    if (int rc = setup_round0(s)) return rc;
+    if (!use_graph) return run_plain(s);
+    const u64 key = ((u64)B << 40) ^ ((u64)N << 2) ^ ((u64)(uintptr_t)d_T) ^ ((u64)(uintptr_t)d_L << 1) ^
+                    ((u64)(uintptr_t)d_I << 3) ^ ((u64)(uintptr_t)d_SA << 5) ^ (u64)cfg.tile_cap ^ ((u64)Ncap << 7);
+    if (!gexec || key != graph_key) {
+        if (int rc = build_graph(s)) return rc;
+        graph_key = key;
+    }
+    KGB_CHECK(cudaGraphLaunch(gexec, s));
+    stats.launches = -1;
+    return 0;
+}
+
+int FwdEngine::error_flag(cudaStream_t s, u32 *err) {
+    KGB_CHECK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    KGB_CHECK(cudaStreamSynchronize(s));
+    *err = h_ctl->err;
+    stats.rounds = (int)h_ctl->round;
+    return 0;
+}
+
+}  // namespace kgb

@@ -1,0 +1,144 @@
+// Forward BWT engine: prefix-doubling suffix sorting of a batch of independent blocks on one GPU.
+#pragma once
+#include "common.cuh"
+
+#include <vector>
+
+namespace kgb {
+
+struct FwdArgs;
+
+// One block of a batch. `off` is the block's first byte in the concatenated text; the block's L column (n + 1
+// bytes, sentinel row included) starts at off + index of the block; its sampled indexes start at `iout`.
+struct BlockInfo {
+    u32 off, n, r, iout;
+};
+
+// A segment of an element list: `len` consecutive elements starting at `start` that form one group (equal sort
+// keys so far) whose first member sits at suffix-array position `head` of block `bd & 0xFFFFFF`. The top byte of
+// `bd` holds the next radix digit for segments still being split by the bucket passes.
+struct Seg {
+    u32 start, len, head, bd;
+};
+
+enum : u32 {
+    L_S0, L_S1,  // small groups (<= SMAX elements), one list per round parity
+    L_L0, L_L1,  // large groups, one list per round parity
+    L_K0, L_K1,  // bucket-pass work lists (ping-pong across passes)
+    L_KS,        // small buckets produced by the bucket passes, keys attached
+    L_R0, L_R1,  // suffixes resolved in a round (their ranks are copied to the other rank buffer next round)
+    NLISTS
+};
+
+struct ListView {
+    u32 *eid;   // element: global suffix index
+    u32 *ekey;  // element: current sort key (rank rounds), may be null
+    Seg *seg;   // segment descriptors
+    u32 *tmap;  // tile map (see fwd.cu)
+};
+
+// Device-resident control block of one forward sort (read by every kernel, written by the 1-thread control
+// kernels), so that the whole sort can run inside a CUDA graph without host round trips.
+struct Ctl {
+    u64 cnt[NLISTS];  // per list: (segments << 32) | elements
+    u32 rpar;         // round parity
+    u32 pass;         // bucket pass within the round
+    u32 round;        // doubling round (0: 8-byte prefixes)
+    u32 h;            // characters already sorted (rank rounds)
+    u32 done;
+    u32 err;
+    u32 maxrounds;
+    u32 pad;
+};
+
+struct FwdConfig {
+    int tile_cap = 4096;  // small-group tile capacity: 4096 or 8192 (groups up to tile_cap / 2 go to the tiles)
+    int tile_ctas = 2;    // persistent CTAs per SM for the tile sorter
+    int msd_ctas = 4;     // persistent CTAs per SM for the bucket passes
+};
+
+struct FwdStats {
+    int rounds;
+    int passes;
+    long long launches;
+    double ms;
+};
+
+// Device buffers for batches up to (ncap bytes, bcap blocks). Reused across calls; grown on demand.
+class FwdEngine {
+   public:
+    FwdEngine();
+    ~FwdEngine();
+    // Prepares a batch of `count` blocks with lengths n[] (each >= 2) and sampling intervals r[]: lays the blocks
+    // out, grows the buffers and fills the block table. Returns 0, -1 (too large) or -2 (out of device memory).
+    int plan(const u32 *n, const u32 *r, int count, bool want_sa);
+    // Device text buffer of the planned batch (block b at offsets()[b]); 16 zero bytes follow the last block.
+    u8 *text() const { return d_T; }
+    const std::vector<u32> &offsets() const { return h_off; }
+    const std::vector<u32> &iouts() const { return h_iout; }
+    u64 total() const { return N; }
+    u32 samples() const { return nI; }
+    // Runs the sort on `s`: graph = one CUDA-graph launch with device-side loops, else one launch per kernel with a
+    // host read of the control block after each round and bucket pass. Results stay on the device.
+    int run(cudaStream_t s, bool graph);
+    // Result buffers (device): L columns (block b at off + b, n + 1 bytes), sampled indexes, suffix arrays.
+    const u8 *lcol() const { return d_L; }
+    const u32 *samples_dev() const { return d_I; }
+    const u32 *sa_dev() const { return d_SA; }
+    int error_flag(cudaStream_t s, u32 *err);  // reads the device error word (after run)
+    u64 workspace_bytes() const { return pool_bytes; }
+    FwdConfig cfg;
+    FwdStats stats{};
+
+    // External-buffer mode: sort texts already on the device (dT: concatenated texts, 16 readable bytes past the
+    // last; dL / dI / dSA receive the results). Lays the batch out from caller offsets.
+    int plan_external(const u32 *off, const u32 *n, const u32 *r, const u32 *iout, int count, u8 *dT, u8 *dL,
+                      u32 *dI, u32 *dSA);
+
+   private:
+    int grow(u64 ncap, u32 bcap, u32 icap, bool want_sa);
+    int run_plain(cudaStream_t s);
+    int run_graph(cudaStream_t s);
+    int build_graph(cudaStream_t s);
+    void free_all();
+    int setup_round0(cudaStream_t s);
+    void set_caps(FwdArgs &a) const;
+    u64 cap_segs = 0, cap_segl = 0, cap_tms = 0, cap_tml = 0;
+
+    // capacities
+    u64 Ncap = 0;
+    u32 Bcap = 0, Icap = 0;
+    bool sa_cap = false;
+    // planned batch
+    u64 N = 0;
+    u32 B = 0, nI = 0;
+    u32 maxn = 0;
+    std::vector<u32> h_off, h_n, h_r, h_iout;
+    bool ext = false;
+    bool want_sa_run = false;
+
+    // device buffers
+    u8 *d_T = nullptr, *d_L = nullptr;
+    u8 *own_T = nullptr, *own_L = nullptr;
+    u32 *d_I = nullptr, *own_I = nullptr;
+    u32 *d_SA = nullptr, *own_SA = nullptr;
+    u32 *d_isa[2] = {nullptr, nullptr};
+    BlockInfo *d_blk = nullptr;
+    ListView lists[NLISTS];
+    u32 *d_hist = nullptr, *d_cursor = nullptr, *d_bhead = nullptr, *d_orand = nullptr;
+    u8 *d_dest = nullptr;
+    Ctl *d_ctl = nullptr;
+    Ctl *h_ctl = nullptr;  // pinned mirror
+    void *pool = nullptr;
+    size_t pool_bytes = 0;
+
+    // graph cache
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int graph_cap_key = 0;
+    u64 graph_key = 0;
+    int sm_count = 0;
+    int grid_tile = 0, grid_msd = 0, grid_scan = 0;
+};
+
+}  // namespace kgb

@@ -1,0 +1,487 @@
+// Inverse BWT on the GPU (sm_103a): psi table by a stable counting sort, then a parallel walk of many short chains.
+//
+// Conventions are the reference's (src/algo/sais/sais.c:12055-12082, the LF walk of tests/bwt_reference.py:270-290
+// in adnaneben/kolmo): the L column is U with the sentinel re-inserted at row p0 = I[0]; row 0 of the sorted matrix
+// is the sentinel rotation. Instead of LF (backwards) this decodes forwards with psi = LF^-1:
+//   F row x holds the first byte of the suffix at row x, psi[x] is the row of the next suffix,
+//   T[0] = F(p0), T[j + 1] = F(psi^(j+1)(p0)), and the walk ends at row 0 (the suffix of length 0).
+// psi is built by a stable counting sort of the L column by byte (psi[C[c] + k] = row of the k-th c in L).
+//
+// Parallel decode (the chain idea of libsais's split decoder, sais.c:11573-11703, re-designed for a GPU):
+//   * rows p0 and every multiple of MARK are marks; bit 31 of psi[x] flags "psi[x] is a mark" so a walk learns it
+//     reached the next mark from the load it needs anyway;
+//   * one chain per mark walks psi until the next mark (or row 0), writing its bytes into its own CAPC-byte
+//     buffer; a walk that reaches CAPC bytes closes its chain and continues as a new chain, so buffers never overflow
+//     and no row is walked twice;
+//   * chains are ranked by pointer jumping over (successor, length); a chain's text position is n minus its
+//     distance to the end of the text;
+//   * chains are copied to their positions.
+// A string that is not a valid BWT has more than one psi cycle: the walk from p0 then reaches row 0 before n bytes.
+// That block is reported (-1) instead of decoded. Every loop is bounded by the number of rows.
+#include "inv.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace kgb {
+
+constexpr int ITPB = 256;
+constexpr u32 ITILE = 4096;
+constexpr u32 MARK = 64;
+constexpr u32 CAPC = 256;
+constexpr u32 ENDC = 0xFFFFFFFFu;
+constexpr u32 CHUNK = 2048;  // start chains per walk work item
+constexpr int KSLOT = 4;     // chains walked at once by one thread
+
+struct InvArgs {
+    const u8 *U;
+    u8 *out;
+    u32 *psi;
+    u32 *thist;
+    const u32 *tblk;
+    u32 *C;
+    const InvBlock *blk;
+    u32 B;
+    u64 ntiles;
+    u64 nchains;
+    u32 *len, *succ, *dyn, *status;
+    u32 *nx[2], *dist[2];
+    u8 *buf;
+    const u32 *chunks;
+    u32 nchunks;
+    u32 jpar;
+    u64 cap_n;  // bytes of the text buffers (checked build)
+};
+
+__device__ __forceinline__ u32 is_mark(u32 q, u32 p0) { return q != 0 && (q % MARK == 0 || q == p0); }
+
+// Per-tile byte histograms.
+__global__ void __launch_bounds__(ITPB) k_inv_tilehist(InvArgs a) {
+    __shared__ u32 h[256];
+    const u32 lane = lane_id();
+    for (u64 t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const InvBlock B = a.blk[a.tblk[t]];
+        const u32 start = (u32)(t - B.tile_base) * ITILE;
+        const u32 cnt = min(ITILE, B.n - start);
+        h[threadIdx.x] = 0;
+        __syncthreads();
+        for (u32 i0 = 0; i0 < ITILE; i0 += ITPB) {
+            const u32 i = i0 + threadIdx.x;
+            const u32 c = i < cnt ? (u32)a.U[(u64)B.off + start + i] : 0x100u;
+            const u32 peers = __match_any_sync(0xffffffffu, c);
+            if (c < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[c], __popc(peers));
+        }
+        __syncthreads();
+        a.thist[t * 256 + threadIdx.x] = h[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// Per block: column-wise exclusive scan of the tile histograms plus the C array (C[c] = 1 + number of bytes below
+// c: F row 0 is the sentinel), so thist[t][c] becomes the first psi slot of tile t's c bytes.
+__global__ void __launch_bounds__(ITPB) k_inv_colscan(InvArgs a) {
+    __shared__ u32 ws[ITPB / 32 + 1];
+    const u32 c = threadIdx.x;
+    for (u32 b = blockIdx.x; b < a.B; b += gridDim.x) {
+        const InvBlock B = a.blk[b];
+        u32 tot = 0;
+        for (u32 lt = 0; lt < B.ntiles; lt++) tot += a.thist[((u64)B.tile_base + lt) * 256 + c];
+        u32 all;
+        const u32 cc = 1 + block_excl_sum<ITPB>(tot, ws, &all);
+        a.C[(u64)b * 257 + c] = cc;
+        if (c == 255) a.C[(u64)b * 257 + 256] = 1 + all;
+        u32 run = cc;
+        for (u32 lt = 0; lt < B.ntiles; lt++) {
+            const u64 idx = ((u64)B.tile_base + lt) * 256 + c;
+            const u32 v = a.thist[idx];
+            a.thist[idx] = run;
+            run += v;
+        }
+        if (c == 0) a.psi[(u64)B.off + b] = B.p0 | 0x80000000u;  // psi[0]: the sentinel row leads to row p0
+    }
+}
+
+// Stable scatter: psi[C[c] + occurrences of c before row q] = q, with the mark flag of q.
+__global__ void __launch_bounds__(ITPB) k_inv_scatter(InvArgs a) {
+    constexpr int NW = ITPB / 32, IPT = ITILE / ITPB, WS = 32 * IPT;
+    __shared__ u16 wc[NW][256];
+    __shared__ u32 woff[NW][256];
+    const u32 lane = lane_id(), warp = warp_id();
+    for (u64 t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const u32 b = a.tblk[t];
+        const InvBlock B = a.blk[b];
+        const u32 start = (u32)(t - B.tile_base) * ITILE;
+        const u32 cnt = min(ITILE, B.n - start);
+        for (int i = threadIdx.x; i < NW * 256; i += ITPB) (&wc[0][0])[i] = 0;
+        __syncthreads();
+        u32 cs[IPT], rk[IPT];
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const u32 x = warp * WS + j * 32 + lane;
+            const u32 c = x < cnt ? (u32)a.U[(u64)B.off + start + x] : 0x100u;
+            cs[j] = c;
+            const u32 peers = __match_any_sync(0xffffffffu, c);
+            const u32 before = c < 256 ? wc[warp][c] : 0u;
+            rk[j] = before + __popc(peers & lanemask_lt());
+            __syncwarp();
+            if (c < 256 && (__ffs(peers) - 1) == (int)lane) wc[warp][c] = (u16)(before + __popc(peers));
+            __syncwarp();
+        }
+        __syncthreads();
+        {
+            u32 run = a.thist[t * 256 + threadIdx.x];
+#pragma unroll
+            for (int w = 0; w < NW; w++) { woff[w][threadIdx.x] = run; run += wc[w][threadIdx.x]; }
+        }
+        __syncthreads();
+        u32 *psi = a.psi + (u64)B.off + b;
+#pragma unroll
+        for (int j = 0; j < IPT; j++) {
+            const u32 x = warp * WS + j * 32 + lane;
+            if (x < cnt) {
+                const u32 u = start + x;
+                const u32 q = u + (u >= B.p0);
+                const u32 dst = woff[warp][cs[j]] + rk[j];
+                KGB_GUARD(dst >= 1 && dst <= B.n, &a.status[b], 0x100) psi[dst] = q | (is_mark(q, B.p0) << 31);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ u32 f_of(const u32 *Cs, u32 row) {  // largest c with C[c] <= row
+    u32 lo = 0;
+#pragma unroll
+    for (u32 step = 128; step; step >>= 1)
+        if (Cs[lo + step] <= row) lo += step;
+    return lo;
+}
+
+// Walk every chain of a work item (block, [c0, c1) start chains). Chain 0 starts at p0; chain m >= 1 at row m*MARK
+// (none when that row is p0). Chains that reach CAPC bytes continue under a new id taken from the block's counter.
+__global__ void __launch_bounds__(ITPB) k_inv_walk(InvArgs a) {
+    __shared__ u32 Cs[257];
+    for (u32 w = blockIdx.x; w < a.nchunks; w += gridDim.x) {
+        const u32 b = a.chunks[3 * w], c0 = a.chunks[3 * w + 1], c1 = a.chunks[3 * w + 2];
+        const InvBlock B = a.blk[b];
+        __syncthreads();
+        for (u32 i = threadIdx.x; i < 257; i += ITPB) Cs[i] = a.C[(u64)b * 257 + i];
+        __syncthreads();
+        const u32 *psi = a.psi + (u64)B.off + b;
+        u32 next = c0 + threadIdx.x;
+        u32 row[KSLOT], steps[KSLOT], acc[KSLOT], cid[KSLOT];
+        bool act[KSLOT];
+#pragma unroll
+        for (int k = 0; k < KSLOT; k++) {
+            act[k] = false;
+            while (next < c1) {
+                const u32 id = next;
+                next += ITPB;
+                const u32 start = id == 0 ? B.p0 : id * MARK;
+                if (id != 0 && start == B.p0) continue;  // chain 0 covers the mark at p0
+                row[k] = start; steps[k] = 0; acc[k] = 0; cid[k] = id; act[k] = true;
+                break;
+            }
+        }
+        for (;;) {
+            bool any = false;
+            u32 v[KSLOT];
+#pragma unroll
+            for (int k = 0; k < KSLOT; k++)
+                if (act[k]) { v[k] = __ldg(psi + row[k]); any = true; }
+            if (!any) break;
+#pragma unroll
+            for (int k = 0; k < KSLOT; k++) {
+                if (!act[k]) continue;
+                const u64 g = (u64)B.chain_base + cid[k];
+                const u32 c = f_of(Cs, row[k]);
+                acc[k] |= c << (8 * (steps[k] & 3));
+                if ((steps[k] & 3) == 3) {
+                    reinterpret_cast<u32 *>(a.buf + g * CAPC)[steps[k] >> 2] = acc[k];
+                    acc[k] = 0;
+                }
+                steps[k]++;
+                u32 nxt = v[k] & 0x7FFFFFFFu;
+                if (nxt > B.n) {  // psi entries are rows 0..n: anything else is an internal error
+                    a.status[b] = 3;
+                    nxt = 0;
+                }
+                const bool stop = (v[k] >> 31) || nxt == 0;
+                if (stop || steps[k] == CAPC) {
+                    if (steps[k] & 3) reinterpret_cast<u32 *>(a.buf + g * CAPC)[steps[k] >> 2] = acc[k];
+                    a.len[g] = steps[k];
+                    if (stop) {
+                        a.succ[g] = nxt == 0 ? ENDC : B.chain_base + (nxt == B.p0 ? 0u : nxt / MARK);
+                        act[k] = false;
+                        while (next < c1) {
+                            const u32 id = next;
+                            next += ITPB;
+                            const u32 start = id == 0 ? B.p0 : id * MARK;
+                            if (id != 0 && start == B.p0) continue;
+                            row[k] = start; steps[k] = 0; acc[k] = 0; cid[k] = id; act[k] = true;
+                            break;
+                        }
+                    } else {
+                        const u32 nid = B.nreg + 1 + atomicAdd(&a.dyn[b], 1u);
+                        if (nid >= B.chain_cap) {  // cannot happen for any input: each record covers CAPC rows
+                            a.status[b] = 2;
+                            a.succ[g] = ENDC;
+                            act[k] = false;
+                        } else {
+                            a.succ[g] = B.chain_base + nid;
+                            cid[k] = nid; row[k] = nxt; steps[k] = 0; acc[k] = 0;
+                        }
+                    }
+                } else {
+                    row[k] = nxt;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_inv_rank_init(InvArgs a) {
+    for (u64 g = (u64)blockIdx.x * blockDim.x + threadIdx.x; g < a.nchains; g += (u64)gridDim.x * blockDim.x) {
+        a.nx[0][g] = a.succ[g];
+        a.dist[0][g] = a.len[g];
+    }
+}
+
+// One pointer-jumping step: dist[g] += dist[nx[g]], nx[g] = nx[nx[g]] (saturating; chains off the main path may
+// form cycles and are discarded later).
+__global__ void k_inv_jump(InvArgs a) {
+    const u32 *nxi = a.nx[a.jpar], *di = a.dist[a.jpar];
+    u32 *nxo = a.nx[a.jpar ^ 1], *dout = a.dist[a.jpar ^ 1];
+    for (u64 g = (u64)blockIdx.x * blockDim.x + threadIdx.x; g < a.nchains; g += (u64)gridDim.x * blockDim.x) {
+        const u32 x = nxi[g];
+        const u32 d = di[g];
+        if (x == ENDC) { nxo[g] = ENDC; dout[g] = d; continue; }
+        const u64 s = (u64)d + di[x];
+        nxo[g] = nxi[x];
+        dout[g] = s > 0xFFFFFFFFull ? 0xFFFFFFFFu : (u32)s;
+    }
+}
+
+// Copy every chain on the main path to its text position (one warp per chain) and set the block status.
+__global__ void k_inv_emit(InvArgs a) {
+    const u32 lane = lane_id();
+    const u32 *nx = a.nx[a.jpar], *dist = a.dist[a.jpar];
+    const u64 wid = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 g = wid; g < a.nchains; g += nw) {
+        u32 lo = 0, hi = a.B - 1;  // block of chain g: last block with chain_base <= g
+        while (lo < hi) {
+            u32 mid = (lo + hi + 1) >> 1;
+            if (a.blk[mid].chain_base <= g) lo = mid; else hi = mid - 1;
+        }
+        const InvBlock B = a.blk[lo];
+        if (g >= (u64)B.chain_base + B.chain_cap) continue;
+        const u32 x = nx[g], d = dist[g], L = a.len[g];
+        if (g == B.chain_base && lane == 0 && a.status[lo] != 2) a.status[lo] = (x == ENDC && d == B.n) ? 0 : 1;
+        if (x != ENDC || L == 0 || d > B.n || L > d) continue;
+        const u64 dst = (u64)B.off + (B.n - d);
+        const u8 *src = a.buf + g * CAPC;
+        if (!KGB_OK(L <= CAPC && dst + L <= a.cap_n, &a.status[lo], 0x100)) continue;
+        for (u32 i = lane; i < L; i += 32) a.out[dst + i] = src[i];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ host engine
+static size_t ialign(size_t x, size_t al) { return (x + al - 1) / al * al; }
+
+InvEngine::InvEngine() {}
+InvEngine::~InvEngine() { free_all(); }
+
+void InvEngine::free_all() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    gexec = nullptr; graph = nullptr;
+    if (pool) cudaFree(pool);
+    pool = nullptr;
+    if (h_status) cudaFreeHost(h_status);
+    h_status = nullptr;
+    Ncap = Tcap = Ccap = 0; Bcap = 0;
+}
+
+int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
+    if (ncap <= Ncap && bcap <= Bcap && tcap <= Tcap && ccap <= Ccap) return 0;
+    ncap = std::max(ncap, Ncap); bcap = std::max(bcap, Bcap); tcap = std::max(tcap, Tcap); ccap = std::max(ccap, Ccap);
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (pool) { cudaFree(pool); pool = nullptr; }
+    struct Item { void **p; size_t bytes; };
+    std::vector<Item> items;
+    auto add = [&](void **p, size_t bytes) { items.push_back({p, ialign(std::max<size_t>(bytes, 16), 256)}); };
+    add((void **)&own_U, ncap + 64);
+    add((void **)&own_out, ncap + 64);
+    add((void **)&d_psi, (ncap + bcap + 16) * 4);
+    add((void **)&d_thist, tcap * 256 * 4);
+    add((void **)&d_tblk, tcap * 4);
+    add((void **)&d_C, (size_t)bcap * 257 * 4);
+    add((void **)&d_blk, (size_t)bcap * sizeof(InvBlock));
+    add((void **)&d_len, ccap * 4);
+    add((void **)&d_succ, ccap * 4);
+    add((void **)&d_nx[0], ccap * 4);
+    add((void **)&d_nx[1], ccap * 4);
+    add((void **)&d_dist[0], ccap * 4);
+    add((void **)&d_dist[1], ccap * 4);
+    add((void **)&d_buf, ccap * CAPC);
+    add((void **)&d_dyn, (size_t)bcap * 4);
+    add((void **)&d_status, (size_t)bcap * 4);
+    add((void **)&d_chunks, (ccap / CHUNK + bcap + 8) * 12);
+    size_t total = 0;
+    for (auto &it : items) total += it.bytes;
+    cudaError_t e = cudaMalloc(&pool, total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        pool = nullptr;
+        Ncap = 0;
+        return record_cuda_error(e, "cudaMalloc(inverse workspace)", __FILE__, __LINE__);
+    }
+    pool_bytes = total;
+    size_t off = 0;
+    for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
+    if (h_status) cudaFreeHost(h_status);
+    KGB_CHECK(cudaMallocHost(&h_status, (size_t)bcap * sizeof(int)));
+    Ncap = ncap; Bcap = bcap; Tcap = tcap; Ccap = ccap;
+    return 0;
+}
+
+static int plan_layout(const u32 *off, const u32 *n, const u32 *p0, int count, std::vector<InvBlock> &blk,
+                       std::vector<u32> &tblk, std::vector<u32> &chunks, u64 &ntiles, u64 &nchains, u32 &maxchains) {
+    blk.resize(count);
+    tblk.clear();
+    chunks.clear();
+    ntiles = 0; nchains = 0; maxchains = 0;
+    for (int b = 0; b < count; b++) {
+        if (n[b] < 2 || p0[b] < 1 || p0[b] > n[b]) return -1;
+        InvBlock B;
+        B.off = off[b]; B.n = n[b]; B.p0 = p0[b];
+        B.tile_base = (u32)ntiles;
+        B.ntiles = (n[b] + ITILE - 1) / ITILE;
+        B.nreg = n[b] / MARK;
+        B.chain_base = (u32)nchains;
+        B.chain_cap = B.nreg + 1 + n[b] / CAPC + 4;
+        for (u32 t = 0; t < B.ntiles; t++) tblk.push_back((u32)b);
+        for (u32 c = 0; c < B.nreg + 1; c += CHUNK) {
+            chunks.push_back((u32)b); chunks.push_back(c); chunks.push_back(std::min(B.nreg + 1, c + CHUNK));
+        }
+        ntiles += B.ntiles;
+        nchains += B.chain_cap;
+        maxchains = std::max(maxchains, B.chain_cap);
+        blk[b] = B;
+        if (ntiles > 0xFFFF0000ull || nchains > 0xFFFF0000ull) return -1;
+    }
+    return 0;
+}
+
+int InvEngine::plan(const u32 *n, const u32 *p0, int count) {
+    if (count <= 0) return -1;
+    h_off.resize(count);
+    u64 off = 0;
+    for (int b = 0; b < count; b++) {
+        h_off[b] = (u32)off;
+        off += ((u64)n[b] + 15) / 16 * 16;
+        if (off > 0xFFFF0000ull) return -1;
+    }
+    std::vector<u32> tblk;
+    if (plan_layout(h_off.data(), n, p0, count, h_blk, tblk, h_chunks, ntiles, nchains, maxchains)) return -1;
+    N = off; B = (u32)count;
+    int rc = grow(N, B, ntiles, nchains);
+    if (rc) return rc;
+    ext = false;
+    d_U = own_U; d_out = own_out;
+    KGB_CHECK(cudaMemcpy(d_tblk, tblk.data(), tblk.size() * 4, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int InvEngine::plan_external(const u32 *off, const u32 *n, const u32 *p0, int count, u8 *dU, u8 *dOut) {
+    if (count <= 0) return -1;
+    h_off.assign(off, off + count);
+    std::vector<u32> tblk;
+    if (plan_layout(off, n, p0, count, h_blk, tblk, h_chunks, ntiles, nchains, maxchains)) return -1;
+    u64 end = 0;
+    for (int b = 0; b < count; b++) end = std::max<u64>(end, (u64)off[b] + n[b]);
+    N = end; B = (u32)count;
+    int rc = grow(N, B, ntiles, nchains);
+    if (rc) return rc;
+    ext = true;
+    d_U = dU; d_out = dOut;
+    KGB_CHECK(cudaMemcpy(d_tblk, tblk.data(), tblk.size() * 4, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int InvEngine::enqueue(cudaStream_t s, long long *launches) {
+    InvArgs a;
+    memset(&a, 0, sizeof(a));
+    a.U = d_U; a.out = d_out; a.psi = d_psi; a.thist = d_thist; a.tblk = d_tblk; a.C = d_C; a.blk = d_blk; a.B = B;
+    a.ntiles = ntiles; a.nchains = nchains; a.len = d_len; a.succ = d_succ; a.dyn = d_dyn; a.status = d_status;
+    a.nx[0] = d_nx[0]; a.nx[1] = d_nx[1]; a.dist[0] = d_dist[0]; a.dist[1] = d_dist[1]; a.buf = d_buf;
+    a.chunks = d_chunks; a.nchunks = nchunks; a.jpar = 0; a.cap_n = Ncap;
+    const int g4 = sm_count * 4;
+    KGB_CHECK(cudaMemsetAsync(d_len, 0, nchains * 4, s));
+    KGB_CHECK(cudaMemsetAsync(d_succ, 0xFF, nchains * 4, s));
+    KGB_CHECK(cudaMemsetAsync(d_dyn, 0, (size_t)B * 4, s));
+    KGB_CHECK(cudaMemsetAsync(d_status, 0, (size_t)B * 4, s));
+    k_inv_tilehist<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a);
+    k_inv_colscan<<<(int)std::min<u32>(B, 4096u), ITPB, 0, s>>>(a);
+    k_inv_scatter<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a);
+    k_inv_walk<<<(int)std::min<u32>(nchunks, (u32)sm_count * 8), ITPB, 0, s>>>(a);
+    k_inv_rank_init<<<g4, 256, 0, s>>>(a);
+    *launches += 5;
+    for (u32 j = 0; j < njump; j++) {
+        a.jpar = j & 1;
+        k_inv_jump<<<g4, 256, 0, s>>>(a);
+        (*launches)++;
+    }
+    a.jpar = njump & 1;
+    k_inv_emit<<<g4, 256, 0, s>>>(a);
+    (*launches)++;
+    KGB_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int InvEngine::run(cudaStream_t s, bool use_graph) {
+    stats = InvStats{};
+    if (!sm_count) {
+        int dev;
+        KGB_CHECK(cudaGetDevice(&dev));
+        KGB_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+    }
+    nchunks = (u32)(h_chunks.size() / 3);
+    njump = 1;
+    while ((1ull << njump) < (u64)maxchains + 1) njump++;
+    njump += 1;
+    stats.jumps = (int)njump;
+    KGB_CHECK(cudaMemcpyAsync(d_blk, h_blk.data(), h_blk.size() * sizeof(InvBlock), cudaMemcpyHostToDevice, s));
+    KGB_CHECK(cudaMemcpyAsync(d_chunks, h_chunks.data(), h_chunks.size() * 4, cudaMemcpyHostToDevice, s));
+    KGB_CHECK(cudaStreamSynchronize(s));  // host vectors are pageable: finish before they can change
+    if (!use_graph) return enqueue(s, &stats.launches);
+    const u64 key = ((u64)B << 40) ^ N ^ ((u64)(uintptr_t)d_U << 1) ^ ((u64)(uintptr_t)d_out << 3) ^ (ntiles << 17) ^
+                    (nchains << 23) ^ ((u64)njump << 58) ^ ((u64)nchunks << 29) ^ (Ncap << 11);
+    if (!gexec || key != graph_key) {
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        KGB_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        long long dummy = 0;
+        int rc = enqueue(s, &dummy);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        KGB_CHECK(e);
+        graph = g;
+        KGB_CHECK(cudaGraphInstantiate(&gexec, graph, 0));
+        graph_key = key;
+    }
+    KGB_CHECK(cudaGraphLaunch(gexec, s));
+    stats.launches = -1;
+    return 0;
+}
+
+int InvEngine::fetch_status(cudaStream_t s, std::vector<int> &status) {
+    KGB_CHECK(cudaMemcpyAsync(h_status, d_status, (size_t)B * sizeof(int), cudaMemcpyDeviceToHost, s));
+    KGB_CHECK(cudaStreamSynchronize(s));
+    status.assign(h_status, h_status + B);
+    return 0;
+}
+
+}  // namespace kgb

@@ -1,0 +1,70 @@
+// Inverse BWT engine: parallel psi-walk decode of a batch of blocks on one GPU.
+#pragma once
+#include "common.cuh"
+
+#include <vector>
+
+namespace kgb {
+
+struct InvBlock {
+    u32 off;         // first byte of the block's BWT string (and of its decoded text)
+    u32 n;           // block length
+    u32 p0;          // primary index (row of the sentinel in the L column), 1..n
+    u32 tile_base;   // first 4096-byte tile of the block
+    u32 ntiles;
+    u32 chain_base;  // first chain record of the block
+    u32 nreg;        // regular marks (rows M, 2M, ..., nreg * M)
+    u32 chain_cap;   // chain records reserved for the block
+};
+
+struct InvStats {
+    long long launches;
+    int jumps;
+};
+
+class InvEngine {
+   public:
+    InvEngine();
+    ~InvEngine();
+    // blocks of lengths n[] (>= 2) with primary indexes p0[] in 1..n. Returns 0, -1 or -2.
+    int plan(const u32 *n, const u32 *p0, int count);
+    int plan_external(const u32 *off, const u32 *n, const u32 *p0, int count, u8 *dU, u8 *dOut);
+    u8 *input() const { return d_U; }
+    const u8 *output() const { return d_out; }
+    const std::vector<u32> &offsets() const { return h_off; }
+    u64 total() const { return N; }
+    // decode on stream s; per-block status (0 ok, -1 not a valid BWT) lands in status() after sync
+    int run(cudaStream_t s, bool graph);
+    int fetch_status(cudaStream_t s, std::vector<int> &status);
+    InvStats stats{};
+    u64 workspace_bytes() const { return pool_bytes; }
+
+   private:
+    int grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap);
+    int build_graph(cudaStream_t s);
+    int enqueue(cudaStream_t s, long long *launches);
+    void free_all();
+    u64 Ncap = 0, Tcap = 0, Ccap = 0;
+    u32 Bcap = 0;
+    u64 N = 0, ntiles = 0, nchains = 0;
+    u32 B = 0, maxchains = 0, njump = 0, nchunks = 0;
+    std::vector<u32> h_off;
+    std::vector<InvBlock> h_blk;
+    std::vector<u32> h_chunks;  // (block, first chain, end chain) triples for the walk
+    bool ext = false;
+    u8 *d_U = nullptr, *d_out = nullptr, *own_U = nullptr, *own_out = nullptr;
+    u32 *d_psi = nullptr, *d_thist = nullptr, *d_C = nullptr, *d_tblk = nullptr;
+    u32 *d_len = nullptr, *d_succ = nullptr, *d_nx[2] = {nullptr, nullptr}, *d_dist[2] = {nullptr, nullptr};
+    u32 *d_dyn = nullptr, *d_status = nullptr, *d_chunks = nullptr;
+    u8 *d_buf = nullptr;
+    InvBlock *d_blk = nullptr;
+    void *pool = nullptr;
+    size_t pool_bytes = 0;
+    int *h_status = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    u64 graph_key = 0;
+    int sm_count = 0;
+};
+
+}  // namespace kgb

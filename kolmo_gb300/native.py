@@ -1,0 +1,92 @@
+"""ctypes bindings to ``libkgbwt.so``, the C ABI of the GPU block-sorting engine (``include/kgbwt.h``).
+
+The library is loaded from the package's ``_native`` directory (built in-tree by ``kolmo_gb300.build``). There is no
+CPU fallback: if the library is missing or cannot load, every call raises.
+Set ``KGBWT_CHECKED=1`` to load the bounds-checked build instead (same ABI; device writes are range-checked).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_U32 = ctypes.c_uint32
+
+
+class FwdJob(ctypes.Structure):
+    _fields_ = [("T", _P), ("U", _P), ("n", _I32), ("r", _I32), ("I", _P), ("rc", _I32)]
+
+
+class InvJob(ctypes.Structure):
+    _fields_ = [("T", _P), ("U", _P), ("n", _I32), ("r", _I32), ("I", _P), ("rc", _I32)]
+
+
+class Block(ctypes.Structure):
+    _fields_ = [("off", _U32), ("n", _U32), ("r", _U32), ("iout", _U32)]
+
+
+class IBlock(ctypes.Structure):
+    _fields_ = [("off", _U32), ("n", _U32), ("p0", _U32), ("pad", _U32)]
+
+
+PLAIN = 1
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB_CHECKED if os.environ.get("KGBWT_CHECKED") == "1" else _build.LIB
+
+
+def lib():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"kgbwt CUDA library not built: {path} (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    L.kolmo_sais_bwt_aux.argtypes = [_P, _P, _P, _I32, _I32, _P, _I32]
+    L.kolmo_sais_bwt_aux.restype = _I32
+    L.kolmo_sais_unbwt_aux.argtypes = [_P, _P, _P, _I32, _I32, _P, _I32]
+    L.kolmo_sais_unbwt_aux.restype = _I32
+    L.kolmo_sais_unbwt.argtypes = [_P, _P, _P, _I32, _I32, _I32]
+    L.kolmo_sais_unbwt.restype = _I32
+    L.kgbwt_fwd_batch.argtypes = [ctypes.POINTER(FwdJob), _I32, _U32]
+    L.kgbwt_fwd_batch.restype = _I32
+    L.kgbwt_inv_batch.argtypes = [ctypes.POINTER(InvJob), _I32, _U32]
+    L.kgbwt_inv_batch.restype = _I32
+    L.kgbwt_engine_create.restype = _P
+    L.kgbwt_engine_destroy.argtypes = [_P]
+    L.kgbwt_engine_config.argtypes = [_P, _I32, _I32, _I32]
+    L.kgbwt_engine_config.restype = _I32
+    L.kgbwt_engine_fwd.argtypes = [_P, _P, _P, _P, _P, ctypes.POINTER(Block), _I32, _P, _U32]
+    L.kgbwt_engine_fwd.restype = _I32
+    L.kgbwt_engine_inv.argtypes = [_P, _P, _P, ctypes.POINTER(IBlock), _I32, _P, _U32]
+    L.kgbwt_engine_inv.restype = _I32
+    L.kgbwt_engine_wait.argtypes = [_P, _P]
+    L.kgbwt_engine_wait.restype = _I32
+    L.kgbwt_engine_stats.argtypes = [_P, _P, _P, _P]
+    L.kgbwt_engine_stats.restype = _I32
+    L.kgbwt_engine_workspace_bytes.argtypes = [_P]
+    L.kgbwt_engine_workspace_bytes.restype = ctypes.c_uint64
+    L.kgbwt_last_error.restype = ctypes.c_char_p
+    L.kgbwt_version.restype = _I32
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().kgbwt_last_error().decode(errors="replace")
+
+
+# the exported symbols include/kgbwt.h declares (the CPU tests check that the library exports each of them)
+EXPORTS = (
+    "kolmo_sais_bwt_aux", "kolmo_sais_unbwt_aux", "kolmo_sais_unbwt", "kgbwt_fwd_batch", "kgbwt_inv_batch",
+    "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
+    "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
+)
