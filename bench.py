@@ -1,0 +1,461 @@
+"""Benchmark of the GPU BWT path: one step = forward BWT + inverse BWT of one block.
+
+Default workload (the single-block configuration): a 64 MiB block of Zipf(1.1) word-token prose (50k-word
+vocabulary, 2% random bytes, 200 verbatim 4-64 KiB repeats), seeded synthetic data standing in for the reference's
+text corpora. The codec-18 sampling interval for the block (2^23, 7 samples) is used.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload prose64|batch]
+
+Output: one JSON line on rank 0.
+  value   MiB/s of forward+inverse with the input resident in HBM, timed with CUDA events on the engine's stream,
+          L2 flushed (a 256 MiB write) between steps, whole job over all ranks (each rank sorts its own block:
+          weak scaling, no collective on the data path);
+  e2e     the same metric through the reference-facing C ABI (kolmo_sais_bwt_aux + kolmo_sais_unbwt_aux) with
+          pinned host buffers, host<->device copies inside the timed region;
+  roofline   the dominant kernel (largest share of device time in a profiled pass of one step, CUDA events around
+          every launch of the plain path on the same stream) against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU sorter timed on this host's cores on a bounded sample of the same workload.
+--impl reference times the reference's own CPU sorter (built from its sources where the reference tree was present,
+else the CPU restatement in oracle/) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+MIB = 1 << 20
+HBM_FALLBACK_GBS = 6800.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+# ------------------------------------------------------------------------------------------------ distributed
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world: int, backend: str):
+    import torch.distributed as dist
+
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def reduce_max(x: float, world: int, device=None) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(items: list, rank: int, world: int) -> list:
+    """Longest-first assignment of independent blocks to ranks (the reference's claim_block order,
+    src/core/blocks.c:148-178), returning this rank's share."""
+    order = sorted(range(len(items)), key=lambda i: -items[i])
+    load = [0] * world
+    mine = []
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        load[r] += items[i]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
+
+
+# ------------------------------------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------------ CPU sorter
+def cpu_sorter():
+    """(kind, callable fwd(T, r) -> (rc, U, I), inv(U, r, I) -> (rc, T), threads): the reference's own sorter when
+    it was built on a machine like this one and loads here, else the CPU restatement."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    if O.ref_lib() is not None:
+        return ("reference", lambda T, r: O.bwt_aux(T, r, use_ref=True, threads=threads),
+                lambda U, r, I: O.unbwt_aux(U, r, I, use_ref=True, threads=threads), threads)
+    return ("port", lambda T, r: O.bwt_aux(T, r), lambda U, r, I: O.unbwt_aux(U, r, I), 1)
+
+
+def time_cpu(T: np.ndarray, r: int, budget_s: float, max_reps: int = 3):
+    """fwd+inv MiB/s of the CPU sorter on T (repeated while the budget allows)."""
+    kind, fwd, inv, threads = cpu_sorter()
+    reps, total = 0, 0.0
+    while reps < max_reps:
+        t0 = time.perf_counter()
+        rc, U, I = fwd(T, r)
+        rc2, back = inv(U, r, I)
+        total += time.perf_counter() - t0
+        reps += 1
+        assert rc == 0 and rc2 == 0 and np.array_equal(back, T), "CPU sorter failed its round trip"
+        if total > budget_s:
+            break
+    return kind, threads, reps * T.size / MIB / total, reps
+
+
+# ------------------------------------------------------------------------------------------------ workloads
+def prose_block(rank: int, mib: int = 64):
+    from kolmo_gb300 import workloads as W
+
+    if rank == 0:
+        return W.prose_64mib(mib * MIB)
+    return W.zipf_prose(mib * MIB, W.SEED_PROSE_64MIB + rank)
+
+
+def algorithmic_bytes(rec: dict) -> float:
+    """Algorithmic bytes of one launch (the per-unit figures of the doubling model): a rank round costs 48 B per
+    active suffix (read its id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id),
+    round 0 33 B per suffix, the inverse 10 B per byte over its passes (psi build: read L, write psi; walk: read psi,
+    write text)."""
+    k, e = rec["kernel"], rec["elems"]
+    if k in ("tile_sort_rank", "tile_sort_rank_keyed"):
+        return 48.0 * e
+    if k in ("tile_sort_prefix", "tile_sort_prefix_keyed"):
+        return 33.0 * e
+    if k == "inv_walk":
+        return 5.0 * e   # read psi 4 B + write 1 B per decoded byte
+    if k == "inv_scatter":
+        return 5.0 * e   # read L 1 B + write psi 4 B per byte
+    if k in ("msd_hist",):
+        return 8.0 * e
+    if k in ("msd_scatter",):
+        return 16.0 * e
+    if k == "keygen":
+        return 12.0 * e
+    return 0.0
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from kolmo_gb300 import codec, native
+    from kolmo_gb300.host import codec18_rlog, n_samples
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    T = prose_block(rank, args.block_mib)
+    n = int(T.size)
+    r = 1 << codec18_rlog(n)
+    ns = n_samples(n, r)
+    s = torch.cuda.Stream(device=dev)
+    eng = codec.Engine()
+    dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
+    dT[:n] = torch.from_numpy(T).to(dev)
+    dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
+    dI = torch.zeros(ns, dtype=torch.int32, device=dev)
+    dU = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
+    dOut = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * MIB, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step(plain=False):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(s)
+        rc = eng.fwd(dT, dL, dI, [(0, n, r, 0)], stream=s, plain=plain)
+        ev[1].record(s)
+        rc2 = eng.wait()[0]
+        if rc or rc2:
+            raise RuntimeError(f"forward failed: {rc} {rc2} {native.last_error()}")
+        p0 = int(dI[0].item())
+        ev[2].record(s)
+        with torch.cuda.stream(s):
+            dU[:p0].copy_(dL[:p0])
+            dU[p0:n].copy_(dL[p0 + 1:n + 1])
+        rc = eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=plain)
+        ev[3].record(s)
+        rc2, st = eng.wait(1)
+        if rc or rc2:
+            raise RuntimeError(f"inverse failed: {rc} {rc2} {native.last_error()}")
+        return ev
+
+    # warm-up (also the correctness check of this run)
+    for _ in range(max(args.warmup, 1)):
+        step()
+    s.synchronize()
+    assert torch.equal(dOut[:n], dT[:n]), "round trip failed"
+    if rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    times, tf, ti = [], [], []
+    for _ in range(args.steps):
+        with torch.cuda.stream(s):
+            flush.fill_(1)
+        ev = step()
+        s.synchronize()
+        tf.append(ev[0].elapsed_time(ev[1]))
+        ti.append(ev[2].elapsed_time(ev[3]))
+        times.append(ev[0].elapsed_time(ev[3]))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = reduce_max(sum(times), world, dev)
+    value = world * args.steps * n / MIB / (total_ms / 1e3)
+    if args.skip_extras:  # timed steps only (profiler runs)
+        return {"metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+                "block_bytes": n, "skip_extras": True}
+
+    # profiled pass (plain path, CUDA events around every launch on stream s)
+    eng.profile(True)
+    step(plain=True)
+    prof_f = eng.profile_read()
+    s.synchronize()
+    p0 = int(dI[0].item())
+    eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True)
+    eng.wait(1)
+    prof_i = eng.profile_read()
+    eng.profile(False)
+    launches_fwd = sum(1 for x in prof_f)
+    launches_inv = sum(1 for x in prof_i)
+    prof = prof_f + prof_i
+    by_kernel = {}
+    for rec in prof:
+        d = by_kernel.setdefault(rec["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0.0})
+        d["launches"] += 1
+        d["ms"] += rec["ms"]
+        d["bytes"] += algorithmic_bytes(rec)
+    tot_ms = sum(d["ms"] for d in by_kernel.values())
+    dom = max((k for k in by_kernel if k != "control"), key=lambda k: by_kernel[k]["ms"])
+    dd = by_kernel[dom]
+    peak, peak_kind = peaks()
+    achieved = dd["bytes"] / dd["launches"] / (dd["ms"] / dd["launches"] / 1e3) / 1e9 if dd["ms"] > 0 else 0.0
+    rounds = {}
+    for rec in prof_f:
+        rr = rounds.setdefault(rec["round"], {"ms": 0.0, "m": 0})
+        rr["ms"] += rec["ms"]
+        if rec["kernel"] in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_sort_prefix", "tile_sort_prefix_keyed"):
+            rr["m"] += rec["elems"]
+    round_table = []
+    for j in sorted(rounds):
+        m = rounds[j]["m"] if j > 0 else n
+        b = (48.0 if j > 0 else 33.0) * m
+        ms = rounds[j]["ms"]
+        round_table.append({"round": j, "h": 0 if j == 0 else 8 << (j - 1), "m": m, "ms": round(ms, 4),
+                            "GBs": round(b / (ms / 1e3) / 1e9, 1) if ms > 0 else None})
+
+    # e2e through the drop-in C ABI with pinned host buffers
+    e2e = run_e2e(T, r, args.steps, max(args.warmup, 1), world, dev)
+
+    out = {
+        "metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "prose64: one 64 MiB Zipf(1.1) word-token prose block per GPU, forward + inverse BWT",
+                   "block_bytes": n, "r": r, "samples": ns, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas{world}", "tile_cap": 4096},
+        "fwd_MiB_per_s": round(args.steps * n / MIB / (sum(tf) / 1e3), 2),
+        "inv_MiB_per_s": round(args.steps * n / MIB / (sum(ti) / 1e3), 2),
+        "e2e": e2e,
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "launches_per_step": dd["launches"], "share": round(dd["ms"] / tot_ms, 4),
+                     "bytes_model": "rank round 48 B per active suffix, round 0 33 B per suffix (per launch: "
+                                    "elements of the launch's work list)"},
+        "kernel_shares": {k: round(v["ms"] / tot_ms, 4) for k, v in sorted(by_kernel.items(), key=lambda x: -x[1]["ms"])},
+        "rounds": round_table,
+        "gpu_launches": args.steps * (launches_fwd + launches_inv),
+        "clocks": clk,
+    }
+    if traffic_path := os.environ.get("KGBWT_TRAFFIC_JSON"):
+        try:
+            out["roofline"]["traffic"] = json.load(open(traffic_path)).get(dom)
+        except Exception:
+            pass
+    if rank == 0:
+        kind, threads, cpu_v, reps = time_cpu(T[: 16 * MIB], r, budget_s=12.0)
+        out["cpu_baseline"] = {"value": round(cpu_v, 2), "unit": "MiB/s", "cores": threads, "kind": kind,
+                               "sample": f"first 16 MiB of the block, forward+inverse, {reps} run(s), r={r}"}
+    return out
+
+
+def run_e2e(T, r, steps, warmup, world, dev):
+    import torch
+
+    from kolmo_gb300 import native
+    from kolmo_gb300.host import n_samples
+
+    L = native.lib()
+    n = int(T.size)
+    Th = torch.from_numpy(T.copy()).pin_memory()
+    Uh = torch.empty(n, dtype=torch.uint8).pin_memory()
+    Bh = torch.empty(n, dtype=torch.uint8).pin_memory()
+    I = np.zeros(n_samples(n, r), np.int32)
+    A = np.zeros(1, np.int32)
+    tp, up, bp = Th.data_ptr(), Uh.data_ptr(), Bh.data_ptr()
+
+    def one():
+        rc = L.kolmo_sais_bwt_aux(tp, up, A.ctypes.data, n, r, I.ctypes.data, 1)
+        rc2 = L.kolmo_sais_unbwt_aux(up, bp, A.ctypes.data, n, r, I.ctypes.data, 1)
+        if rc or rc2:
+            raise RuntimeError(f"C ABI round trip failed: {rc} {rc2} {native.last_error()}")
+
+    for _ in range(warmup):
+        one()
+    assert torch.equal(Bh, Th), "C ABI round trip differs"
+    barrier(world)
+    t = 0.0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        one()
+        t += time.perf_counter() - t0
+    t = reduce_max(t, world, dev)
+    return {"value": round(world * steps * n / MIB / t, 2), "unit": "MiB/s", "h2d_bytes_per_step": 2 * n,
+            "d2h_bytes_per_step": (n + 1) + 4 * int(I.size) + n,
+            "path": "kolmo_sais_bwt_aux + kolmo_sais_unbwt_aux, pinned host buffers"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    T = prose_block(0)
+    from kolmo_gb300.host import codec18_rlog
+
+    r = 1 << codec18_rlog(T.size)
+    kind, fwd, inv, threads = cpu_sorter()
+    # size the per-step sample so that warm-up + steps stay within about two minutes
+    probe = T[: 4 * MIB]
+    t0 = time.perf_counter()
+    rc, U, I = fwd(probe, r)
+    inv(U, r, I)
+    speed = probe.size / (time.perf_counter() - t0)  # bytes/s
+    per_step = 120.0 / max(args.steps + args.warmup, 1)
+    sample = int(min(T.size, max(4 * MIB, speed * per_step)))
+    S = T[:sample]
+    for _ in range(args.warmup):
+        fwd(S, r)
+    t = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rc, U, I = fwd(S, r)
+        rc2, back = inv(U, r, I)
+        t += time.perf_counter() - t0
+        assert rc == 0 and rc2 == 0
+    v = args.steps * sample / MIB / t
+    desc = f"first {sample / MIB:.1f} MiB of the 64 MiB prose block per step, forward+inverse, r={r}"
+    return {"metric": "bwt_fwd_inv_MiB_per_s", "value": round(v, 2), "unit": "MiB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "prose64: one 64 MiB Zipf(1.1) word-token prose block, forward + inverse BWT",
+                       "block_bytes": int(T.size), "r": r, "parallelism": "cpu"},
+            "cpu_baseline": {"value": round(v, 2), "unit": "MiB/s", "cores": threads, "kind": kind, "sample": desc},
+            "e2e": {"value": round(v, 2), "unit": "MiB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="prose64", choices=["prose64"])
+    ap.add_argument("--block-mib", type=int, default=64, help="block size (the benchmark configuration is 64)")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="timed steps only: no e2e, profiled pass or CPU baseline (for profiler captures)")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    import torch
+
+    dist_init(world, "nccl" if torch.cuda.is_available() else "gloo")
+    out = run_ours(args, world, rank, local)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

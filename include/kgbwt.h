@@ -101,6 +101,22 @@ int32_t kgbwt_engine_stats(kgbwt_engine *e, int32_t *rounds, int32_t *passes, in
 /* Device bytes held by the engine's workspaces. */
 uint64_t kgbwt_engine_workspace_bytes(kgbwt_engine *e);
 
+/* Kernel profile of the engine's plain-path calls (flag KGBWT_PLAIN): with profiling enabled every kernel launch is
+ * bracketed by CUDA events on the call's stream. After kgbwt_engine_wait, kgbwt_engine_profile_read copies up to
+ * cap records of the last call and returns their number. kernel is an id named by kgbwt_kernel_name; elems / segs
+ * are the size of the launch's input (elements and groups of its work list; bytes or chain records for the inverse). */
+typedef struct {
+    int32_t kernel;
+    int32_t round;
+    int32_t pass;
+    uint32_t elems;
+    uint32_t segs;
+    float ms;
+} kgbwt_prof;
+int32_t kgbwt_engine_profile(kgbwt_engine *e, int32_t enable);
+int32_t kgbwt_engine_profile_read(kgbwt_engine *e, kgbwt_prof *out, int32_t cap);
+const char *kgbwt_kernel_name(int32_t kernel);
+
 /* ---- misc --------------------------------------------------------------------------------------------------------- */
 const char *kgbwt_last_error(void); /* text of the last error on this thread ("" if none) */
 int32_t kgbwt_version(void);

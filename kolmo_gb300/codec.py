@@ -18,7 +18,7 @@ _DUMMY_A = np.zeros(1, np.int32)  # the caller's scratch: checked for NULL like 
 
 
 def n_samples(n: int, r: int) -> int:
-    return (n - 1) // r + 1 if n > 0 else 1
+    return (n - 1) // r + 1 if n > 0 and r > 0 else 1
 
 
 def _u8(a) -> np.ndarray:
@@ -148,6 +148,18 @@ class Engine:
         r, p, l = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
         native.lib().kgbwt_engine_stats(self.h, ctypes.byref(r), ctypes.byref(p), ctypes.byref(l))
         return {"rounds": r.value, "passes": p.value, "launches": l.value}
+
+    def profile(self, enable: bool = True):
+        native.lib().kgbwt_engine_profile(self.h, 1 if enable else 0)
+
+    def profile_read(self):
+        """Records of the last plain-path call: list of dicts (kernel, round, pass, elems, segs, ms)."""
+        L = native.lib()
+        n = L.kgbwt_engine_profile_read(self.h, None, 0)
+        buf = (native.Prof * max(n, 1))()
+        n = L.kgbwt_engine_profile_read(self.h, buf, n)
+        return [{"kernel": L.kgbwt_kernel_name(r.kernel).decode(), "round": r.round, "pass": r.pass_,
+                 "elems": r.elems, "segs": r.segs, "ms": r.ms} for r in buf[:n]]
 
     def workspace_bytes(self) -> int:
         return int(native.lib().kgbwt_engine_workspace_bytes(self.h))

@@ -15,6 +15,14 @@ namespace kgb {
 
 static thread_local char g_err[512];
 
+const char *kernel_name(int k) {
+    static const char *names[K_NKERNELS] = {
+        "init", "fixup", "keygen", "msd_hist", "msd_scan", "msd_scatter", "tile_sort_prefix", "tile_sort_prefix_keyed",
+        "tile_sort_rank", "tile_sort_rank_keyed", "control", "samples",
+        "inv_tilehist", "inv_colscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
+    return k >= 0 && k < K_NKERNELS ? names[k] : "?";
+}
+
 void record_error(const char *msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
 
 int record_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
@@ -84,7 +92,6 @@ static uint32_t env_flags() {
 static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
-    if (int rc = C.init()) return rc;
     std::vector<int> dev;
     std::vector<u32> n, r;
     for (int i = 0; i < count; i++) {
@@ -101,7 +108,8 @@ static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
         n.push_back((u32)j.n);
         r.push_back((u32)j.r);
     }
-    if (dev.empty()) return 0;
+    if (dev.empty()) return 0;  // argument errors and n <= 1 never touch the device
+    if (int rc = C.init()) { for (int i : dev) jobs[i].rc = rc; return rc; }
     FwdEngine &E = C.eng.fwd;
     int rc = E.plan(n.data(), r.data(), (int)dev.size(), false);
     if (rc) { for (int i : dev) jobs[i].rc = rc; return rc; }
@@ -144,7 +152,6 @@ static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
 static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
-    if (int rc = C.init()) return rc;
     std::vector<int> dev;
     std::vector<u32> n, p0;
     for (int i = 0; i < count; i++) {
@@ -166,6 +173,7 @@ static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
         p0.push_back((u32)j.I[0]);
     }
     if (dev.empty()) return 0;
+    if (int rc = C.init()) { for (int i : dev) jobs[i].rc = rc; return rc; }
     InvEngine &E = C.eng.inv;
     int rc = E.plan(n.data(), p0.data(), (int)dev.size());
     auto fail = [&](int code) { for (int i : dev) jobs[i].rc = code; return code; };
@@ -328,6 +336,29 @@ int32_t kgbwt_engine_stats(kgbwt_engine *e, int32_t *rounds, int32_t *passes, in
 }
 
 uint64_t kgbwt_engine_workspace_bytes(kgbwt_engine *e) { return e ? e->fwd.workspace_bytes() + e->inv.workspace_bytes() : 0; }
+
+int32_t kgbwt_engine_profile(kgbwt_engine *e, int32_t enable) {
+    if (!e) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    e->fwd.prof.on = enable != 0;
+    e->inv.prof.on = enable != 0;
+    return 0;
+}
+
+int32_t kgbwt_engine_profile_read(kgbwt_engine *e, kgbwt_prof *out, int32_t cap) {
+    if (!e || (!out && cap)) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    Profiler &P = e->last_kind == 2 ? e->inv.prof : e->fwd.prof;
+    P.finish();
+    int32_t k = 0;
+    for (const ProfRec &r : P.recs) {
+        if (k >= cap) break;
+        out[k++] = kgbwt_prof{r.kernel, r.round, r.pass, r.elems, r.segs, r.ms};
+    }
+    return (int32_t)P.recs.size();
+}
+
+const char *kgbwt_kernel_name(int32_t kernel) { return kernel_name(kernel); }
 
 const char *kgbwt_last_error(void) { return g_err; }
 int32_t kgbwt_version(void) { return 100; }

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace kgb {
 
 typedef uint8_t u8;
@@ -112,5 +114,59 @@ __device__ __forceinline__ u64 load_be64(const u8 *__restrict__ T, u64 i) {
     u32 lo = (u32)w, hi = (u32)(w >> 32);
     return ((u64)__byte_perm(lo, 0, 0x0123) << 32) | (u64)__byte_perm(hi, 0, 0x0123);
 }
+
+// ---- host-side kernel profiler: CUDA events around every launch of the plain path, tagged with the kernel, the
+// round and the size of the kernel's input (elements and segments of its work list).
+enum KernelId : int {
+    K_INIT, K_FIXUP, K_KEYGEN, K_MSD_HIST, K_MSD_SCAN, K_MSD_SCATTER, K_TILE_PREFIX, K_TILE_PREFIX_KEYED,
+    K_TILE_RANK, K_TILE_RANK_KEYED, K_CTL, K_SAMPLES,
+    K_INV_TILEHIST, K_INV_COLSCAN, K_INV_SCATTER, K_INV_WALK, K_INV_RANKINIT, K_INV_JUMP, K_INV_EMIT, K_NKERNELS
+};
+const char *kernel_name(int k);
+
+struct ProfRec {
+    int kernel, round, pass;
+    u32 elems, segs;
+    cudaEvent_t e0, e1;
+    float ms;
+};
+
+struct Profiler {
+    bool on = false;
+    std::vector<ProfRec> recs;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    int kernel = 0, round = 0, pass = 0;
+    u32 elems = 0, segs = 0;
+    void tag(int k, u32 e, u32 sg = 0) { kernel = k; elems = e; segs = sg; }
+    void reset() { recs.clear(); used = 0; }
+    cudaEvent_t ev() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    // wraps one launch
+    template <typename F>
+    cudaError_t launch(cudaStream_t s, F fn) {
+        if (!on) return fn();
+        ProfRec r{kernel, round, pass, elems, segs, ev(), ev(), 0.f};
+        if (r.e0) cudaEventRecord(r.e0, s);
+        cudaError_t e = fn();
+        if (r.e1) cudaEventRecord(r.e1, s);
+        recs.push_back(r);
+        return e;
+    }
+    // after the stream has synchronised
+    void finish() {
+        for (auto &r : recs)
+            if (r.e0 && r.e1 && cudaEventElapsedTime(&r.ms, r.e0, r.e1) != cudaSuccess) r.ms = -1.f;
+    }
+    ~Profiler() {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
 
 }  // namespace kgb

@@ -968,12 +968,17 @@ struct Launcher {
     cudaStream_t s;
     int grid_tile, grid_msd, grid_scan, tile_cap;
     long long *launches;
+    Profiler *prof;
     template <typename K, typename... Args>
     cudaError_t go(K kern, int grid, int block, size_t smem, Args... args) {
-        kern<<<grid, block, smem, s>>>(args...);
         (*launches)++;
-        return cudaGetLastError();
+        auto fn = [&]() -> cudaError_t {
+            kern<<<grid, block, smem, s>>>(args...);
+            return cudaGetLastError();
+        };
+        return prof ? prof->launch(s, fn) : fn();
     }
+    void tag(int k, u32 e, u32 sg = 0) { if (prof) prof->tag(k, e, sg); }
 };
 
 static bool g_attr_done[4] = {false, false, false, false};
@@ -997,6 +1002,7 @@ static int set_tile_attrs(int tile) {
 
 // Kernel sequences shared by the plain and graph paths.
 static cudaError_t enq_tile(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
+    if (L.prof) L.prof->kernel = prefix ? (keyed ? K_TILE_PREFIX_KEYED : K_TILE_PREFIX) : (keyed ? K_TILE_RANK_KEYED : K_TILE_RANK);
     if (L.tile_cap == 4096) {
         const size_t sm = tile_smem<4096>();
         if (prefix) return keyed ? L.go(k_tile_sort<true, true, 4096>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<true, false, 4096>, L.grid_tile, TPB, sm, a);
@@ -1008,13 +1014,20 @@ static cudaError_t enq_tile(Launcher &L, const FwdArgs &a, bool prefix, bool key
 }
 static cudaError_t enq_msd_pass(Launcher &L, const FwdArgs &a, bool prefix) {
     cudaError_t e;
+    auto k = [&](int id) { if (L.prof) L.prof->kernel = id; };
     if (prefix) {
+        k(K_MSD_HIST);
         if ((e = L.go(k_msd_hist<true>, L.grid_msd, TPB, 0, a))) return e;
+        k(K_MSD_SCAN);
         if ((e = L.go(k_msd_scan<true>, L.grid_scan, TPB, 0, a))) return e;
+        k(K_MSD_SCATTER);
         return L.go(k_msd_scatter<true>, L.grid_msd, TPB, 0, a);
     }
+    k(K_MSD_HIST);
     if ((e = L.go(k_msd_hist<false>, L.grid_msd, TPB, 0, a))) return e;
+    k(K_MSD_SCAN);
     if ((e = L.go(k_msd_scan<false>, L.grid_scan, TPB, 0, a))) return e;
+    k(K_MSD_SCATTER);
     return L.go(k_msd_scatter<false>, L.grid_msd, TPB, 0, a);
 }
 
@@ -1030,36 +1043,60 @@ int FwdEngine::run_plain(cudaStream_t s) {
     FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
                           B, smax);
     set_caps(a);
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &stats.launches};
+    prof.reset();
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &stats.launches, prof.on ? &prof : nullptr};
+    auto cnt_e = [&](u32 l) { return (u32)h_ctl->cnt[l]; };
+    auto cnt_s = [&](u32 l) { return (u32)(h_ctl->cnt[l] >> 32); };
+    prof.round = 0; prof.pass = 0;
+    L.tag(K_INIT, (u32)N, B);
     KGB_CHECK(L.go(k_init, std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
     auto read_ctl = [&]() -> int {
         KGB_CHECK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
         KGB_CHECK(cudaStreamSynchronize(s));
         return 0;
     };
+    if (int rc = read_ctl()) return rc;
     for (int round = 0;; round++) {
         const bool prefix = round == 0;
-        if (!prefix) KGB_CHECK(L.go(k_fixup, grid_msd, TPB, 0, a));
-        if (!prefix) KGB_CHECK(L.go(k_keygen, grid_msd, TPB, 0, a));
+        const u32 rp = h_ctl->rpar;
+        prof.round = round; prof.pass = -1;
+        if (!prefix) {
+            L.tag(K_FIXUP, cnt_e(L_R0 + (rp ^ 1)));
+            KGB_CHECK(L.go(k_fixup, grid_msd, TPB, 0, a));
+            L.tag(K_KEYGEN, cnt_e(L_L0 + rp), cnt_s(L_L0 + rp));
+            KGB_CHECK(L.go(k_keygen, grid_msd, TPB, 0, a));
+        }
+        L.tag(K_CTL, 0);
         KGB_CHECK(L.go(k_ctl_msd_begin, 1, 1, 0, a));
         if (int rc = read_ctl()) return rc;
-        u32 more = (u32)h_ctl->cnt[L_L0 + h_ctl->rpar] > 0;
+        u32 lin = L_L0 + h_ctl->rpar;
+        u32 more = cnt_e(lin) > 0;
+        int pass = 0;
         while (more) {
+            prof.pass = pass++;
+            L.tag(K_MSD_HIST, cnt_e(lin), cnt_s(lin));
             KGB_CHECK(enq_msd_pass(L, a, prefix));
+            L.tag(K_CTL, 0);
             KGB_CHECK(L.go(k_ctl_msd_next, 1, 1, 0, a));
             stats.passes++;
             if (int rc = read_ctl()) return rc;
             if (h_ctl->err) return report_err(h_ctl->err);
-            more = (u32)h_ctl->cnt[L_K0 + ((h_ctl->pass - 1) & 1)] > 0;
+            lin = L_K0 + ((h_ctl->pass - 1) & 1);
+            more = cnt_e(lin) > 0;
         }
+        prof.pass = -1;
+        if (prof.on) prof.tag(0, cnt_e(L_S0 + h_ctl->rpar), cnt_s(L_S0 + h_ctl->rpar));
         KGB_CHECK(enq_tile(L, a, prefix, false));
+        if (prof.on) prof.tag(0, cnt_e(L_KS), cnt_s(L_KS));
         KGB_CHECK(enq_tile(L, a, prefix, true));
+        L.tag(K_CTL, 0);
         KGB_CHECK(L.go(k_ctl_round_end, 1, 1, 0, a));
         stats.rounds++;
         if (int rc = read_ctl()) return rc;
         if (h_ctl->err) return report_err(h_ctl->err);
         if (h_ctl->done) break;
     }
+    L.tag(K_SAMPLES, nI, B);
     KGB_CHECK(L.go(k_samples, std::min<u32>(B, 1024u), 128, 0, a));
     return 0;
 }
@@ -1148,7 +1185,7 @@ int FwdEngine::build_graph(cudaStream_t s) {
                           B, smax);
     set_caps(a);
     long long dummy = 0;
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &dummy};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &dummy, nullptr};
     Deps deps;
     if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
             return L.go(k_init, (int)std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);

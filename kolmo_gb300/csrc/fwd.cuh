@@ -89,6 +89,7 @@ class FwdEngine {
     u64 workspace_bytes() const { return pool_bytes; }
     FwdConfig cfg;
     FwdStats stats{};
+    Profiler prof;  // plain path only: events around every launch when prof.on
 
     // External-buffer mode: sort texts already on the device (dT: concatenated texts, 16 readable bytes past the
     // last; dL / dI / dSA receive the results). Lays the batch out from caller offsets.

@@ -422,21 +422,25 @@ int InvEngine::enqueue(cudaStream_t s, long long *launches) {
     KGB_CHECK(cudaMemsetAsync(d_succ, 0xFF, nchains * 4, s));
     KGB_CHECK(cudaMemsetAsync(d_dyn, 0, (size_t)B * 4, s));
     KGB_CHECK(cudaMemsetAsync(d_status, 0, (size_t)B * 4, s));
-    k_inv_tilehist<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a);
-    k_inv_colscan<<<(int)std::min<u32>(B, 4096u), ITPB, 0, s>>>(a);
-    k_inv_scatter<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a);
-    k_inv_walk<<<(int)std::min<u32>(nchunks, (u32)sm_count * 8), ITPB, 0, s>>>(a);
-    k_inv_rank_init<<<g4, 256, 0, s>>>(a);
-    *launches += 5;
+    Profiler *P = prof_run ? &prof : nullptr;
+    auto go = [&](int kid, u32 elems, auto fn) -> cudaError_t {
+        (*launches)++;
+        if (!P) { fn(); return cudaGetLastError(); }
+        P->tag(kid, elems);
+        return P->launch(s, [&]() -> cudaError_t { fn(); return cudaGetLastError(); });
+    };
+    const u32 nbytes = (u32)std::min<u64>(N, 0xFFFFFFFFull);
+    KGB_CHECK(go(K_INV_TILEHIST, nbytes, [&] { k_inv_tilehist<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_COLSCAN, (u32)ntiles, [&] { k_inv_colscan<<<(int)std::min<u32>(B, 4096u), ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_SCATTER, nbytes, [&] { k_inv_scatter<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_WALK, nbytes, [&] { k_inv_walk<<<(int)std::min<u32>(nchunks, (u32)sm_count * 8), ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_RANKINIT, (u32)nchains, [&] { k_inv_rank_init<<<g4, 256, 0, s>>>(a); }));
     for (u32 j = 0; j < njump; j++) {
         a.jpar = j & 1;
-        k_inv_jump<<<g4, 256, 0, s>>>(a);
-        (*launches)++;
+        KGB_CHECK(go(K_INV_JUMP, (u32)nchains, [&] { k_inv_jump<<<g4, 256, 0, s>>>(a); }));
     }
     a.jpar = njump & 1;
-    k_inv_emit<<<g4, 256, 0, s>>>(a);
-    (*launches)++;
-    KGB_CHECK(cudaGetLastError());
+    KGB_CHECK(go(K_INV_EMIT, nbytes, [&] { k_inv_emit<<<g4, 256, 0, s>>>(a); }));
     return 0;
 }
 
@@ -455,7 +459,10 @@ int InvEngine::run(cudaStream_t s, bool use_graph) {
     KGB_CHECK(cudaMemcpyAsync(d_blk, h_blk.data(), h_blk.size() * sizeof(InvBlock), cudaMemcpyHostToDevice, s));
     KGB_CHECK(cudaMemcpyAsync(d_chunks, h_chunks.data(), h_chunks.size() * 4, cudaMemcpyHostToDevice, s));
     KGB_CHECK(cudaStreamSynchronize(s));  // host vectors are pageable: finish before they can change
+    prof.reset();
+    prof_run = !use_graph && prof.on;
     if (!use_graph) return enqueue(s, &stats.launches);
+    prof_run = false;
     const u64 key = ((u64)B << 40) ^ N ^ ((u64)(uintptr_t)d_U << 1) ^ ((u64)(uintptr_t)d_out << 3) ^ (ntiles << 17) ^
                     (nchains << 23) ^ ((u64)njump << 58) ^ ((u64)nchunks << 29) ^ (Ncap << 11);
     if (!gexec || key != graph_key) {

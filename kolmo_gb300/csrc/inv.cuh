@@ -37,6 +37,8 @@ class InvEngine {
     int run(cudaStream_t s, bool graph);
     int fetch_status(cudaStream_t s, std::vector<int> &status);
     InvStats stats{};
+    Profiler prof;  // plain path only
+    bool prof_run = false;
     u64 workspace_bytes() const { return pool_bytes; }
 
    private:

@@ -32,6 +32,11 @@ class IBlock(ctypes.Structure):
     _fields_ = [("off", _U32), ("n", _U32), ("p0", _U32), ("pad", _U32)]
 
 
+class Prof(ctypes.Structure):
+    _fields_ = [("kernel", _I32), ("round", _I32), ("pass_", _I32), ("elems", _U32), ("segs", _U32),
+                ("ms", ctypes.c_float)]
+
+
 PLAIN = 1
 
 _lib = None
@@ -74,6 +79,12 @@ def lib():
     L.kgbwt_engine_stats.restype = _I32
     L.kgbwt_engine_workspace_bytes.argtypes = [_P]
     L.kgbwt_engine_workspace_bytes.restype = ctypes.c_uint64
+    L.kgbwt_engine_profile.argtypes = [_P, _I32]
+    L.kgbwt_engine_profile.restype = _I32
+    L.kgbwt_engine_profile_read.argtypes = [_P, ctypes.POINTER(Prof), _I32]
+    L.kgbwt_engine_profile_read.restype = _I32
+    L.kgbwt_kernel_name.argtypes = [_I32]
+    L.kgbwt_kernel_name.restype = ctypes.c_char_p
     L.kgbwt_last_error.restype = ctypes.c_char_p
     L.kgbwt_version.restype = _I32
     _lib = L
@@ -89,4 +100,5 @@ EXPORTS = (
     "kolmo_sais_bwt_aux", "kolmo_sais_unbwt_aux", "kolmo_sais_unbwt", "kgbwt_fwd_batch", "kgbwt_inv_batch",
     "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
     "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
+    "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name",
 )

@@ -80,7 +80,7 @@ def ref_lib():
 
 
 def n_samples(n: int, r: int) -> int:
-    return (n - 1) // r + 1 if n > 0 else 1
+    return (n - 1) // r + 1 if n > 0 and r > 0 else 1
 
 
 def bwt_aux(T: np.ndarray, r: int, use_ref: bool = False, threads: int = 1, want_sa: bool = False):
