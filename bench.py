@@ -221,6 +221,7 @@ def run_ours(args, world, rank, local):
     ns = n_samples(n, r)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group)
     dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
     dT[:n] = torch.from_numpy(T).to(dev)
     dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
@@ -252,7 +253,7 @@ def run_ours(args, world, rank, local):
 
     # warm-up (also the correctness check of this run)
     for _ in range(max(args.warmup, 1)):
-        step()
+        step(plain=args.plain)
     s.synchronize()
     assert torch.equal(dOut[:n], dT[:n]), "round trip failed"
     if rank == 0:
@@ -266,7 +267,7 @@ def run_ours(args, world, rank, local):
     for _ in range(args.steps):
         with torch.cuda.stream(s):
             flush.fill_(1)
-        ev = step()
+        ev = step(plain=args.plain)
         s.synchronize()
         tf.append(ev[0].elapsed_time(ev[1]))
         ti.append(ev[2].elapsed_time(ev[3]))
@@ -279,16 +280,16 @@ def run_ours(args, world, rank, local):
     if args.skip_extras:  # timed steps only (profiler runs)
         return {"metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
-                "block_bytes": n, "skip_extras": True}
+                "fwd_ms": round(sum(tf) / len(tf), 3), "inv_ms": round(sum(ti) / len(ti), 3),
+                "block_bytes": n, "skip_extras": True,
+                "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group]}
 
     # profiled pass (plain path, CUDA events around every launch on stream s)
     eng.profile(True)
-    step(plain=True)
+    assert eng.fwd(dT, dL, dI, [(0, n, r, 0)], stream=s, plain=True) == 0 and eng.wait()[0] == 0
     prof_f = eng.profile_read()
-    s.synchronize()
     p0 = int(dI[0].item())
-    eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True)
-    eng.wait(1)
+    assert eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True) == 0 and eng.wait(1)[0] == 0
     prof_i = eng.profile_read()
     eng.profile(False)
     launches_fwd = sum(1 for x in prof_f)
@@ -436,6 +437,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="prose64", choices=["prose64"])
     ap.add_argument("--block-mib", type=int, default=64, help="block size (the benchmark configuration is 64)")
+    ap.add_argument("--tile-cap", type=int, default=0, help="engine tile capacity (4096 or 8192; 0 = default)")
+    ap.add_argument("--tile-ctas", type=int, default=0)
+    ap.add_argument("--msd-ctas", type=int, default=0)
+    ap.add_argument("--small-group", type=int, default=-1)
+    ap.add_argument("--plain", action="store_true",
+                    help="time the plain path (one launch per kernel, host sync per round) instead of the graph")
     ap.add_argument("--skip-extras", action="store_true",
                     help="timed steps only: no e2e, profiled pass or CPU baseline (for profiler captures)")
     args = ap.parse_args()

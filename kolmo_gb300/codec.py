@@ -103,10 +103,12 @@ class Engine:
         if tile_cap or tile_ctas or msd_ctas:
             self.config(tile_cap, tile_ctas, msd_ctas)
 
-    def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0):
+    def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1):
         rc = native.lib().kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
+        if rc == 0 and small_group >= 0:
+            rc = native.lib().kgbwt_engine_small_group(self.h, small_group)
         if rc:
-            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas}")
+            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group}")
 
     def close(self):
         if self.h:

@@ -19,7 +19,7 @@ const char *kernel_name(int k) {
     static const char *names[K_NKERNELS] = {
         "init", "fixup", "keygen", "msd_hist", "msd_scan", "msd_scatter", "tile_sort_prefix", "tile_sort_prefix_keyed",
         "tile_sort_rank", "tile_sort_rank_keyed", "control", "samples",
-        "inv_tilehist", "inv_colscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
+        "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
 
@@ -261,6 +261,13 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
     }
     if (tile_ctas) e->fwd.cfg.tile_ctas = tile_ctas;
     if (msd_ctas) e->fwd.cfg.msd_ctas = msd_ctas;
+    return 0;
+}
+
+int32_t kgbwt_engine_small_group(kgbwt_engine *e, int32_t small_group) {
+    if (!e || small_group < 0 || small_group > 1024) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    e->fwd.cfg.small_group = small_group;
     return 0;
 }
 

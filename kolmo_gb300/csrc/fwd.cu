@@ -26,6 +26,7 @@
 #include "fwd.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 
@@ -51,6 +52,7 @@ struct FwdArgs {
     u8 *dest;
     u32 B;
     u32 smax;
+    u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segl, cap_tms, cap_tml;
@@ -94,6 +96,7 @@ __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, 
     a.L[(u64)B.off + b + p + 1] = id == B.off ? 0 : __ldg(a.T + id - 1);
     if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
     res.eid[ridx] = id;
+    res.ekey[ridx] = p;
 }
 
 // ------------------------------------------------------------------------------------------------ tile sorter
@@ -101,10 +104,10 @@ __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, 
 // SMAX, so a tile holds at most TILE elements). tmap[t] = index of the first such segment; the producers of a
 // list write it (a segment covering position t * TS writes tmap[t]: its own index if it starts there, else the next).
 
-template <int TILE>
+template <int TILE, typename KeyT>
 struct TileSmem {
     static constexpr int TS = TILE / 2;
-    u64 klo[TILE];
+    KeyT klo[TILE];
     u32 val[TILE];
     u16 khi[TILE];
     u16 wcnt[TPB / 32][256];
@@ -124,11 +127,18 @@ __device__ __forceinline__ void write_tmap_small(const FwdArgs &a, u32 *tmap, u3
     }
 }
 
+template <bool PREFIX, int TILE>
+struct TileTraits {
+    typedef typename std::conditional<PREFIX, u64, u32>::type KeyT;  // rank keys fit 32 bits
+    static constexpr int MINB = TILE == 4096 ? 2 : 1;   // CTAs per SM the registers must allow
+};
+
 template <bool PREFIX, bool KEYED, int TILE>
-__global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
-    constexpr int TS = TILE / 2, IPT = TILE / TPB, WS = 32 * IPT, NW = TPB / 32;
+__global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_sort(FwdArgs a) {
+    typedef typename TileTraits<PREFIX, TILE>::KeyT KeyT;
+    constexpr int TS = TILE / 2, IPT = TILE / TPB, WS = 32 * IPT, NW = TPB / 32, KB = (int)sizeof(KeyT);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    TileSmem<TILE> &S = *reinterpret_cast<TileSmem<TILE> *>(smem_raw);
+    TileSmem<TILE, KeyT> &S = *reinterpret_cast<TileSmem<TILE, KeyT> *>(smem_raw);
     const Ctl *ctl = a.ctl;
     const u32 rpar = ctl->rpar, h = ctl->h;
     const u32 lin = KEYED ? L_KS : L_S0 + rpar;
@@ -172,9 +182,9 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
         __syncthreads();
 
         // ---- load: warp-striped arrangement, x = warp * WS + j * 32 + lane
-        u64 k[IPT];
+        KeyT k[IPT];
         u32 hi[IPT], v[IPT];
-        u64 orl = 0, andl = ~0ull;
+        KeyT orl = 0, andl = (KeyT)~(KeyT)0;
         u32 orh = 0, andh = ~0u;
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
@@ -186,13 +196,14 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
                     u32 mid = (lo + hh + 1) >> 1;
                     if (S.lstart[mid] <= x) lo = mid; else hh = mid - 1;
                 }
-                u64 key;
+                KeyT key;
                 if (PREFIX) {
                     const BlockInfo B = a.blk[S.lblk[lo]];
                     const u64 end = (u64)B.off + B.n;
-                    key = load_be64(a.T, id);
+                    u64 kk = load_be64(a.T, id);
                     const u64 rem = end - id;
-                    if (rem < 8) key &= ~0ull << (8 * (8 - rem));
+                    if (rem < 8) kk &= ~0ull << (8 * (8 - rem));
+                    key = (KeyT)kk;
                 } else if (KEYED) {
                     key = in.ekey[E0 + x];
                 } else {
@@ -204,7 +215,7 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
                 v[j] = id;
                 orl |= key; andl &= key; orh |= lo; andh &= lo;
             } else {
-                k[j] = ~0ull;
+                k[j] = (KeyT)~(KeyT)0;
                 hi[j] = 0xFFFFu;
                 v[j] = 0;
             }
@@ -219,19 +230,57 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
         }
         if (lane == 0) { S.red[0][warp] = orl; S.red[1][warp] = andl; S.red[2][warp] = orh; S.red[3][warp] = andh; }
         __syncthreads();
-        orl = 0; andl = ~0ull; orh = 0; andh = ~0u;
+        orl = 0; andl = (KeyT)~(KeyT)0; orh = 0; andh = ~0u;
 #pragma unroll
         for (int w = 0; w < NW; w++) {
-            orl |= S.red[0][w]; andl &= S.red[1][w]; orh |= (u32)S.red[2][w]; andh &= (u32)S.red[3][w];
+            orl |= (KeyT)S.red[0][w]; andl &= (KeyT)S.red[1][w]; orh |= (u32)S.red[2][w]; andh &= (u32)S.red[3][w];
         }
-        const u64 vary_lo = orl ^ andl;
+        const KeyT vary_lo = orl ^ andl;
         const u32 vary_hi = (orh ^ andh) & 0xFFFFu;
+        // longest group of the tile
+        u32 ml = 0;
+        for (u32 j = tid; j < nsegs; j += TPB) ml = max(ml, S.lstart[j + 1] - S.lstart[j]);
+        ml = block_incl_max<TPB>(ml, S.ws);
+        if (tid == TPB - 1) S.bases[3] = ml;
+        __syncthreads();
+        const u32 maxlen = S.bases[3];
+
+        bool in_smem = false;
+        if (maxlen <= a.small_group && vary_lo) {
+            // ---- small groups: counting sort inside each group (position = keys below + equal keys before)
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                S.klo[x] = k[j];
+            }
+            __syncthreads();
+            u32 dst[IPT];
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                dst[j] = x;
+                if (x < cnt) {
+                    const u32 g0 = S.lstart[hi[j]], g1 = S.lstart[hi[j] + 1];
+                    u32 below = 0;
+                    for (u32 y = g0; y < g1; y++) {
+                        const KeyT ky = S.klo[y];
+                        below += ky < k[j] || (ky == k[j] && y < x);
+                    }
+                    dst[j] = g0 + below;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < IPT; j++) { S.klo[dst[j]] = k[j]; S.khi[dst[j]] = (u16)hi[j]; S.val[dst[j]] = v[j]; }
+            __syncthreads();
+            in_smem = true;
+        }
 
         // ---- LSD radix over the varying bytes: 8 bytes of the key, then 2 bytes of the segment index
-        bool in_smem = false;
-        for (int digit = 0; digit < 10; digit++) {
-            const bool lo_part = digit < 8;
-            const u32 sh = lo_part ? 8 * digit : 8 * (digit - 8);
+        const bool radix = !in_smem;
+        for (int digit = 0; digit < KB + 2 && radix; digit++) {
+            const bool lo_part = digit < KB;
+            const u32 sh = lo_part ? 8 * digit : 8 * (digit - KB);
             if (lo_part ? !((vary_lo >> sh) & 0xFF) : !((vary_hi >> sh) & 0xFF)) continue;
             for (int i = tid; i < NW * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
             __syncthreads();
@@ -291,7 +340,7 @@ __global__ void __launch_bounds__(TPB) k_tile_sort(FwdArgs a) {
             st[j] = en[j] = 0;
             if (x < cnt) {
                 const u32 sj = S.khi[x];
-                const u64 kx = S.klo[x];
+                const KeyT kx = S.klo[x];
                 st[j] = x == S.lstart[sj] || kx != S.klo[x - 1];
                 en[j] = x + 1 == S.lstart[sj + 1] || kx != S.klo[x + 1];
                 if (st[j]) gl = x;
@@ -679,12 +728,8 @@ __global__ void __launch_bounds__(TPB) k_fixup(FwdArgs a) {
     const u32 rpar = ctl->rpar;
     const ListView r = a.lists[L_R0 + (rpar ^ 1)];
     const u32 n = min((u32)ctl->cnt[L_R0 + (rpar ^ 1)], (u32)a.cap_n);
-    const u32 *cur = a.isa[rpar];
     u32 *nxt = a.isa[rpar ^ 1];
-    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) {
-        const u32 id = r.eid[i];
-        nxt[id] = cur[id];
-    }
+    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) nxt[r.eid[i]] = r.ekey[i];
 }
 
 // ------------------------------------------------------------------------------------------------ control
@@ -742,13 +787,12 @@ __global__ void k_samples(FwdArgs a) {
 // Element lists of round 0: blocks up to SMAX bytes are single small groups, longer blocks single large ones.
 // The L column's row 0 (the sentinel rotation) holds the block's last byte.
 __global__ void k_init(FwdArgs a, const u32 *__restrict__ blk_list_start, const u8 *__restrict__ blk_is_large) {
-    const u32 B = a.B;
-    for (u32 b = blockIdx.x; b < B; b += gridDim.x) {
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    for (u32 b = 0; b < a.B; b++) {
         const BlockInfo bi = a.blk[b];
-        const ListView l = a.lists[blk_is_large[b] ? L_L0 : L_S0];
-        const u32 st = blk_list_start[b];
-        for (u32 j = threadIdx.x; j < bi.n; j += blockDim.x) l.eid[st + j] = bi.off + j;
-        if (threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
+        u32 *eid = a.lists[blk_is_large[b] ? L_L0 : L_S0].eid + blk_list_start[b];
+        for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < bi.n; j += stride) eid[j] = bi.off + (u32)j;
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
     }
 }
 
@@ -761,6 +805,8 @@ FwdEngine::FwdEngine() {
 FwdEngine::~FwdEngine() { free_all(); }
 
 void FwdEngine::free_all() {
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     gexec = nullptr;
@@ -804,7 +850,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
         add((void **)&lists[l].eid, n * 4);
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
-        if (!res && l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
+        if (l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
         if (!res) {
             add((void **)&lists[l].seg, (small ? nseg_small : nseg_large) * sizeof(Seg));
             add((void **)&lists[l].tmap, (small ? ntm_small : ntm_large) * 4);
@@ -845,6 +891,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 }
 
 void FwdEngine::set_caps(FwdArgs &a) const {
+    a.small_group = (u32)cfg.small_group;
     a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_tms = cap_tms; a.cap_tml = cap_tml;
 }
 
@@ -961,12 +1008,12 @@ static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const
     return a;
 }
 
-template <int TILE>
-static int tile_smem() { return (int)sizeof(TileSmem<TILE>); }
+template <bool PREFIX, int TILE>
+static int tile_smem() { return (int)sizeof(TileSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
 
 struct Launcher {
     cudaStream_t s;
-    int grid_tile, grid_msd, grid_scan, tile_cap;
+    int grid_tile, grid_msd, grid_scan, tile_cap, grid_tile_prefix;
     long long *launches;
     Profiler *prof;
     template <typename K, typename... Args>
@@ -986,15 +1033,15 @@ static int set_tile_attrs(int tile) {
     int idx = tile == 8192 ? 1 : 0;
     if (g_attr_done[idx]) return 0;
     if (tile == 4096) {
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<true, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<true, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 4096>()));
     } else {
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
-        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<true, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<true, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<true, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 8192>()));
     }
     g_attr_done[idx] = true;
     return 0;
@@ -1004,12 +1051,20 @@ static int set_tile_attrs(int tile) {
 static cudaError_t enq_tile(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
     if (L.prof) L.prof->kernel = prefix ? (keyed ? K_TILE_PREFIX_KEYED : K_TILE_PREFIX) : (keyed ? K_TILE_RANK_KEYED : K_TILE_RANK);
     if (L.tile_cap == 4096) {
-        const size_t sm = tile_smem<4096>();
-        if (prefix) return keyed ? L.go(k_tile_sort<true, true, 4096>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<true, false, 4096>, L.grid_tile, TPB, sm, a);
+        if (prefix) {
+            const size_t sm = tile_smem<true, 4096>();
+            const int g = L.grid_tile_prefix;
+            return keyed ? L.go(k_tile_sort<true, true, 4096>, g, TPB, sm, a) : L.go(k_tile_sort<true, false, 4096>, g, TPB, sm, a);
+        }
+        const size_t sm = tile_smem<false, 4096>();
         return keyed ? L.go(k_tile_sort<false, true, 4096>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<false, false, 4096>, L.grid_tile, TPB, sm, a);
     }
-    const size_t sm = tile_smem<8192>();
-    if (prefix) return keyed ? L.go(k_tile_sort<true, true, 8192>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<true, false, 8192>, L.grid_tile, TPB, sm, a);
+    if (prefix) {
+        const size_t sm = tile_smem<true, 8192>();
+        const int g = L.grid_tile_prefix;
+        return keyed ? L.go(k_tile_sort<true, true, 8192>, g, TPB, sm, a) : L.go(k_tile_sort<true, false, 8192>, g, TPB, sm, a);
+    }
+    const size_t sm = tile_smem<false, 8192>();
     return keyed ? L.go(k_tile_sort<false, true, 8192>, L.grid_tile, TPB, sm, a) : L.go(k_tile_sort<false, false, 8192>, L.grid_tile, TPB, sm, a);
 }
 static cudaError_t enq_msd_pass(Launcher &L, const FwdArgs &a, bool prefix) {
@@ -1044,12 +1099,12 @@ int FwdEngine::run_plain(cudaStream_t s) {
                           B, smax);
     set_caps(a);
     prof.reset();
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &stats.launches, prof.on ? &prof : nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, &stats.launches, prof.on ? &prof : nullptr};
     auto cnt_e = [&](u32 l) { return (u32)h_ctl->cnt[l]; };
     auto cnt_s = [&](u32 l) { return (u32)(h_ctl->cnt[l] >> 32); };
     prof.round = 0; prof.pass = 0;
     L.tag(K_INIT, (u32)N, B);
-    KGB_CHECK(L.go(k_init, std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
+    KGB_CHECK(L.go(k_init, grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
     auto read_ctl = [&]() -> int {
         KGB_CHECK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
         KGB_CHECK(cudaStreamSynchronize(s));
@@ -1185,10 +1240,10 @@ int FwdEngine::build_graph(cudaStream_t s) {
                           B, smax);
     set_caps(a);
     long long dummy = 0;
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, &dummy, nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, &dummy, nullptr};
     Deps deps;
     if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
-            return L.go(k_init, (int)std::min<u32>(B, 4096u), TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
+            return L.go(k_init, L.grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
         }))
         return rc;
     if (int rc = add_round(s, graph, deps, L, a, true, hmsd0, hround)) return rc;
@@ -1212,7 +1267,9 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
         KGB_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
     }
     if (int rc = set_tile_attrs(cfg.tile_cap)) return rc;
-    grid_tile = sm_count * cfg.tile_ctas;
+    // persistent grids: as many CTAs as are resident at once (rank tiles: 3 per SM at 4096, prefix tiles: 2)
+    grid_tile = sm_count * (cfg.tile_cap == 4096 ? std::min(std::max(cfg.tile_ctas, 1), 2) : 1);
+    grid_tile_prefix = sm_count * (cfg.tile_cap == 4096 ? 2 : 1);
     grid_msd = sm_count * cfg.msd_ctas;
     grid_scan = sm_count * 4;
     // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan
@@ -1221,7 +1278,9 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     const u64 key = ((u64)B << 40) ^ ((u64)N << 2) ^ ((u64)(uintptr_t)d_T) ^ ((u64)(uintptr_t)d_L << 1) ^
                     ((u64)(uintptr_t)d_I << 3) ^ ((u64)(uintptr_t)d_SA << 5) ^ (u64)cfg.tile_cap ^ ((u64)Ncap << 7);
     if (!gexec || key != graph_key) {
-        if (int rc = build_graph(s)) return rc;
+        // capture on the engine's own stream: the caller's may be the legacy default stream, which cannot capture
+        if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+        if (int rc = build_graph(cap_stream)) return rc;
         graph_key = key;
     }
     KGB_CHECK(cudaGraphLaunch(gexec, s));

@@ -55,6 +55,7 @@ struct FwdConfig {
     int tile_cap = 4096;  // small-group tile capacity: 4096 or 8192 (groups up to tile_cap / 2 go to the tiles)
     int tile_ctas = 2;    // persistent CTAs per SM for the tile sorter
     int msd_ctas = 4;     // persistent CTAs per SM for the bucket passes
+    int small_group = 64; // tiles whose groups are all at most this long skip the radix passes (counting sort)
 };
 
 struct FwdStats {
@@ -136,10 +137,11 @@ class FwdEngine {
     // graph cache
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    cudaStream_t cap_stream = nullptr;
     int graph_cap_key = 0;
     u64 graph_key = 0;
     int sm_count = 0;
-    int grid_tile = 0, grid_msd = 0, grid_scan = 0;
+    int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0;
 };
 
 }  // namespace kgb

@@ -32,17 +32,18 @@ constexpr u32 CAPC = 256;
 constexpr u32 ENDC = 0xFFFFFFFFu;
 constexpr u32 CHUNK = 2048;  // start chains per walk work item
 constexpr int KSLOT = 4;     // chains walked at once by one thread
+constexpr u32 CHUNKT = 16;   // tiles per chunk of the psi build
 
 struct InvArgs {
     const u8 *U;
     u8 *out;
     u32 *psi;
-    u32 *thist;
-    const u32 *tblk;
+    u32 *csum;
+    const u32 *cblk;
     u32 *C;
     const InvBlock *blk;
     u32 B;
-    u64 ntiles;
+    u64 nchunk_all;
     u64 nchains;
     u32 *len, *succ, *dyn, *status;
     u32 *nx[2], *dist[2];
@@ -55,97 +56,122 @@ struct InvArgs {
 
 __device__ __forceinline__ u32 is_mark(u32 q, u32 p0) { return q != 0 && (q % MARK == 0 || q == p0); }
 
-// Per-tile byte histograms.
-__global__ void __launch_bounds__(ITPB) k_inv_tilehist(InvArgs a) {
+// Per-chunk byte histograms (a chunk is CHUNKT consecutive tiles of one block).
+__global__ void __launch_bounds__(ITPB) k_inv_chunkhist(InvArgs a) {
     __shared__ u32 h[256];
     const u32 lane = lane_id();
-    for (u64 t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const InvBlock B = a.blk[a.tblk[t]];
-        const u32 start = (u32)(t - B.tile_base) * ITILE;
-        const u32 cnt = min(ITILE, B.n - start);
+    for (u64 q = blockIdx.x; q < a.nchunk_all; q += gridDim.x) {
+        const InvBlock B = a.blk[a.cblk[q]];
+        const u32 start = (u32)(q - B.chunk_base) * (ITILE * CHUNKT);
+        const u32 cnt = min(ITILE * CHUNKT, B.n - start);
+        const u8 *src = a.U + (u64)B.off + start;
         h[threadIdx.x] = 0;
         __syncthreads();
-        for (u32 i0 = 0; i0 < ITILE; i0 += ITPB) {
+        for (u32 i0 = 0; i0 < cnt; i0 += ITPB) {
             const u32 i = i0 + threadIdx.x;
-            const u32 c = i < cnt ? (u32)a.U[(u64)B.off + start + i] : 0x100u;
+            const u32 c = i < cnt ? (u32)src[i] : 0x100u;
             const u32 peers = __match_any_sync(0xffffffffu, c);
             if (c < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[c], __popc(peers));
         }
         __syncthreads();
-        a.thist[t * 256 + threadIdx.x] = h[threadIdx.x];
+        a.csum[q * 256 + threadIdx.x] = h[threadIdx.x];
         __syncthreads();
     }
 }
 
-// Per block: column-wise exclusive scan of the tile histograms plus the C array (C[c] = 1 + number of bytes below
-// c: F row 0 is the sentinel), so thist[t][c] becomes the first psi slot of tile t's c bytes.
-__global__ void __launch_bounds__(ITPB) k_inv_colscan(InvArgs a) {
+// Per block: C array (C[c] = 1 + number of bytes below c: F row 0 is the sentinel) and the exclusive scan of the
+// chunk histograms, so csum[q][c] becomes the first psi slot of chunk q's c bytes.
+__global__ void __launch_bounds__(ITPB) k_inv_chunkscan(InvArgs a) {
     __shared__ u32 ws[ITPB / 32 + 1];
     const u32 c = threadIdx.x;
     for (u32 b = blockIdx.x; b < a.B; b += gridDim.x) {
         const InvBlock B = a.blk[b];
+        u32 *col = a.csum + (u64)B.chunk_base * 256 + c;
         u32 tot = 0;
-        for (u32 lt = 0; lt < B.ntiles; lt++) tot += a.thist[((u64)B.tile_base + lt) * 256 + c];
+        u32 q = 0;
+        for (; q + 8 <= B.nchunk; q += 8) {
+            u32 v[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = col[(u64)(q + k) * 256];
+#pragma unroll
+            for (int k = 0; k < 8; k++) tot += v[k];
+        }
+        for (; q < B.nchunk; q++) tot += col[(u64)q * 256];
         u32 all;
         const u32 cc = 1 + block_excl_sum<ITPB>(tot, ws, &all);
         a.C[(u64)b * 257 + c] = cc;
         if (c == 255) a.C[(u64)b * 257 + 256] = 1 + all;
         u32 run = cc;
-        for (u32 lt = 0; lt < B.ntiles; lt++) {
-            const u64 idx = ((u64)B.tile_base + lt) * 256 + c;
-            const u32 v = a.thist[idx];
-            a.thist[idx] = run;
+        q = 0;
+        for (; q + 8 <= B.nchunk; q += 8) {
+            u32 v[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = col[(u64)(q + k) * 256];
+#pragma unroll
+            for (int k = 0; k < 8; k++) { col[(u64)(q + k) * 256] = run; run += v[k]; }
+        }
+        for (; q < B.nchunk; q++) {
+            const u32 v = col[(u64)q * 256];
+            col[(u64)q * 256] = run;
             run += v;
         }
         if (c == 0) a.psi[(u64)B.off + b] = B.p0 | 0x80000000u;  // psi[0]: the sentinel row leads to row p0
     }
 }
 
-// Stable scatter: psi[C[c] + occurrences of c before row q] = q, with the mark flag of q.
+// Stable scatter, one CTA per chunk walking its tiles in order: psi[C[c] + occurrences of c before row q] = q,
+// with the mark flag of q.
 __global__ void __launch_bounds__(ITPB) k_inv_scatter(InvArgs a) {
     constexpr int NW = ITPB / 32, IPT = ITILE / ITPB, WS = 32 * IPT;
     __shared__ u16 wc[NW][256];
     __shared__ u32 woff[NW][256];
+    __shared__ u32 run_s[256];
     const u32 lane = lane_id(), warp = warp_id();
-    for (u64 t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const u32 b = a.tblk[t];
+    for (u64 q = blockIdx.x; q < a.nchunk_all; q += gridDim.x) {
+        const u32 b = a.cblk[q];
         const InvBlock B = a.blk[b];
-        const u32 start = (u32)(t - B.tile_base) * ITILE;
-        const u32 cnt = min(ITILE, B.n - start);
-        for (int i = threadIdx.x; i < NW * 256; i += ITPB) (&wc[0][0])[i] = 0;
-        __syncthreads();
-        u32 cs[IPT], rk[IPT];
-#pragma unroll
-        for (int j = 0; j < IPT; j++) {
-            const u32 x = warp * WS + j * 32 + lane;
-            const u32 c = x < cnt ? (u32)a.U[(u64)B.off + start + x] : 0x100u;
-            cs[j] = c;
-            const u32 peers = __match_any_sync(0xffffffffu, c);
-            const u32 before = c < 256 ? wc[warp][c] : 0u;
-            rk[j] = before + __popc(peers & lanemask_lt());
-            __syncwarp();
-            if (c < 256 && (__ffs(peers) - 1) == (int)lane) wc[warp][c] = (u16)(before + __popc(peers));
-            __syncwarp();
-        }
-        __syncthreads();
-        {
-            u32 run = a.thist[t * 256 + threadIdx.x];
-#pragma unroll
-            for (int w = 0; w < NW; w++) { woff[w][threadIdx.x] = run; run += wc[w][threadIdx.x]; }
-        }
-        __syncthreads();
+        const u32 cstart = (u32)(q - B.chunk_base) * (ITILE * CHUNKT);
+        const u32 ccnt = min(ITILE * CHUNKT, B.n - cstart);
+        run_s[threadIdx.x] = a.csum[q * 256 + threadIdx.x];
         u32 *psi = a.psi + (u64)B.off + b;
+        for (u32 t0 = 0; t0 < ccnt; t0 += ITILE) {
+            const u32 start = cstart + t0;
+            const u32 cnt = min(ITILE, ccnt - t0);
+            for (int i = threadIdx.x; i < NW * 256; i += ITPB) (&wc[0][0])[i] = 0;
+            __syncthreads();
+            u32 cs[IPT], rk[IPT];
 #pragma unroll
-        for (int j = 0; j < IPT; j++) {
-            const u32 x = warp * WS + j * 32 + lane;
-            if (x < cnt) {
-                const u32 u = start + x;
-                const u32 q = u + (u >= B.p0);
-                const u32 dst = woff[warp][cs[j]] + rk[j];
-                KGB_GUARD(dst >= 1 && dst <= B.n, &a.status[b], 0x100) psi[dst] = q | (is_mark(q, B.p0) << 31);
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                const u32 c = x < cnt ? (u32)a.U[(u64)B.off + start + x] : 0x100u;
+                cs[j] = c;
+                const u32 peers = __match_any_sync(0xffffffffu, c);
+                const u32 before = c < 256 ? wc[warp][c] : 0u;
+                rk[j] = before + __popc(peers & lanemask_lt());
+                __syncwarp();
+                if (c < 256 && (__ffs(peers) - 1) == (int)lane) wc[warp][c] = (u16)(before + __popc(peers));
+                __syncwarp();
             }
+            __syncthreads();
+            {
+                u32 run = run_s[threadIdx.x];
+#pragma unroll
+                for (int w = 0; w < NW; w++) { woff[w][threadIdx.x] = run; run += wc[w][threadIdx.x]; }
+                run_s[threadIdx.x] = run;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = warp * WS + j * 32 + lane;
+                if (x < cnt) {
+                    const u32 u = start + x;
+                    const u32 qr = u + (u >= B.p0);
+                    const u32 dst = woff[warp][cs[j]] + rk[j];
+                    KGB_GUARD(dst >= 1 && dst <= B.n, &a.status[b], 0x100) psi[dst] = qr | (is_mark(qr, B.p0) << 31);
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -292,6 +318,8 @@ InvEngine::InvEngine() {}
 InvEngine::~InvEngine() { free_all(); }
 
 void InvEngine::free_all() {
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     gexec = nullptr; graph = nullptr;
@@ -314,8 +342,8 @@ int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
     add((void **)&own_U, ncap + 64);
     add((void **)&own_out, ncap + 64);
     add((void **)&d_psi, (ncap + bcap + 16) * 4);
-    add((void **)&d_thist, tcap * 256 * 4);
-    add((void **)&d_tblk, tcap * 4);
+    add((void **)&d_csum, tcap * 256 * 4);
+    add((void **)&d_cblk, tcap * 4);
     add((void **)&d_C, (size_t)bcap * 257 * 4);
     add((void **)&d_blk, (size_t)bcap * sizeof(InvBlock));
     add((void **)&d_len, ccap * 4);
@@ -347,29 +375,29 @@ int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
 }
 
 static int plan_layout(const u32 *off, const u32 *n, const u32 *p0, int count, std::vector<InvBlock> &blk,
-                       std::vector<u32> &tblk, std::vector<u32> &chunks, u64 &ntiles, u64 &nchains, u32 &maxchains) {
+                       std::vector<u32> &cblk, std::vector<u32> &chunks, u64 &nchunk_all, u64 &nchains, u32 &maxchains) {
     blk.resize(count);
-    tblk.clear();
+    cblk.clear();
     chunks.clear();
-    ntiles = 0; nchains = 0; maxchains = 0;
+    nchunk_all = 0; nchains = 0; maxchains = 0;
     for (int b = 0; b < count; b++) {
         if (n[b] < 2 || p0[b] < 1 || p0[b] > n[b]) return -1;
         InvBlock B;
         B.off = off[b]; B.n = n[b]; B.p0 = p0[b];
-        B.tile_base = (u32)ntiles;
-        B.ntiles = (n[b] + ITILE - 1) / ITILE;
+        B.chunk_base = (u32)nchunk_all;
+        B.nchunk = (n[b] + ITILE * CHUNKT - 1) / (ITILE * CHUNKT);
         B.nreg = n[b] / MARK;
         B.chain_base = (u32)nchains;
         B.chain_cap = B.nreg + 1 + n[b] / CAPC + 4;
-        for (u32 t = 0; t < B.ntiles; t++) tblk.push_back((u32)b);
+        for (u32 t = 0; t < B.nchunk; t++) cblk.push_back((u32)b);
         for (u32 c = 0; c < B.nreg + 1; c += CHUNK) {
             chunks.push_back((u32)b); chunks.push_back(c); chunks.push_back(std::min(B.nreg + 1, c + CHUNK));
         }
-        ntiles += B.ntiles;
+        nchunk_all += B.nchunk;
         nchains += B.chain_cap;
         maxchains = std::max(maxchains, B.chain_cap);
         blk[b] = B;
-        if (ntiles > 0xFFFF0000ull || nchains > 0xFFFF0000ull) return -1;
+        if (nchunk_all > 0xFFFF0000ull || nchains > 0xFFFF0000ull) return -1;
     }
     return 0;
 }
@@ -383,38 +411,38 @@ int InvEngine::plan(const u32 *n, const u32 *p0, int count) {
         off += ((u64)n[b] + 15) / 16 * 16;
         if (off > 0xFFFF0000ull) return -1;
     }
-    std::vector<u32> tblk;
-    if (plan_layout(h_off.data(), n, p0, count, h_blk, tblk, h_chunks, ntiles, nchains, maxchains)) return -1;
+    std::vector<u32> cblk;
+    if (plan_layout(h_off.data(), n, p0, count, h_blk, cblk, h_chunks, nchunk_all, nchains, maxchains)) return -1;
     N = off; B = (u32)count;
-    int rc = grow(N, B, ntiles, nchains);
+    int rc = grow(N, B, nchunk_all, nchains);
     if (rc) return rc;
     ext = false;
     d_U = own_U; d_out = own_out;
-    KGB_CHECK(cudaMemcpy(d_tblk, tblk.data(), tblk.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CHECK(cudaMemcpy(d_cblk, cblk.data(), cblk.size() * 4, cudaMemcpyHostToDevice));
     return 0;
 }
 
 int InvEngine::plan_external(const u32 *off, const u32 *n, const u32 *p0, int count, u8 *dU, u8 *dOut) {
     if (count <= 0) return -1;
     h_off.assign(off, off + count);
-    std::vector<u32> tblk;
-    if (plan_layout(off, n, p0, count, h_blk, tblk, h_chunks, ntiles, nchains, maxchains)) return -1;
+    std::vector<u32> cblk;
+    if (plan_layout(off, n, p0, count, h_blk, cblk, h_chunks, nchunk_all, nchains, maxchains)) return -1;
     u64 end = 0;
     for (int b = 0; b < count; b++) end = std::max<u64>(end, (u64)off[b] + n[b]);
     N = end; B = (u32)count;
-    int rc = grow(N, B, ntiles, nchains);
+    int rc = grow(N, B, nchunk_all, nchains);
     if (rc) return rc;
     ext = true;
     d_U = dU; d_out = dOut;
-    KGB_CHECK(cudaMemcpy(d_tblk, tblk.data(), tblk.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CHECK(cudaMemcpy(d_cblk, cblk.data(), cblk.size() * 4, cudaMemcpyHostToDevice));
     return 0;
 }
 
 int InvEngine::enqueue(cudaStream_t s, long long *launches) {
     InvArgs a;
     memset(&a, 0, sizeof(a));
-    a.U = d_U; a.out = d_out; a.psi = d_psi; a.thist = d_thist; a.tblk = d_tblk; a.C = d_C; a.blk = d_blk; a.B = B;
-    a.ntiles = ntiles; a.nchains = nchains; a.len = d_len; a.succ = d_succ; a.dyn = d_dyn; a.status = d_status;
+    a.U = d_U; a.out = d_out; a.psi = d_psi; a.csum = d_csum; a.cblk = d_cblk; a.C = d_C; a.blk = d_blk; a.B = B;
+    a.nchunk_all = nchunk_all; a.nchains = nchains; a.len = d_len; a.succ = d_succ; a.dyn = d_dyn; a.status = d_status;
     a.nx[0] = d_nx[0]; a.nx[1] = d_nx[1]; a.dist[0] = d_dist[0]; a.dist[1] = d_dist[1]; a.buf = d_buf;
     a.chunks = d_chunks; a.nchunks = nchunks; a.jpar = 0; a.cap_n = Ncap;
     const int g4 = sm_count * 4;
@@ -430,9 +458,10 @@ int InvEngine::enqueue(cudaStream_t s, long long *launches) {
         return P->launch(s, [&]() -> cudaError_t { fn(); return cudaGetLastError(); });
     };
     const u32 nbytes = (u32)std::min<u64>(N, 0xFFFFFFFFull);
-    KGB_CHECK(go(K_INV_TILEHIST, nbytes, [&] { k_inv_tilehist<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a); }));
-    KGB_CHECK(go(K_INV_COLSCAN, (u32)ntiles, [&] { k_inv_colscan<<<(int)std::min<u32>(B, 4096u), ITPB, 0, s>>>(a); }));
-    KGB_CHECK(go(K_INV_SCATTER, nbytes, [&] { k_inv_scatter<<<(int)std::min<u64>(ntiles, (u64)g4 * 2), ITPB, 0, s>>>(a); }));
+    const int gch = (int)std::min<u64>(nchunk_all, (u64)sm_count * 8);
+    KGB_CHECK(go(K_INV_TILEHIST, nbytes, [&] { k_inv_chunkhist<<<gch, ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_COLSCAN, (u32)nchunk_all, [&] { k_inv_chunkscan<<<(int)std::min<u32>(B, 4096u), ITPB, 0, s>>>(a); }));
+    KGB_CHECK(go(K_INV_SCATTER, nbytes, [&] { k_inv_scatter<<<gch, ITPB, 0, s>>>(a); }));
     KGB_CHECK(go(K_INV_WALK, nbytes, [&] { k_inv_walk<<<(int)std::min<u32>(nchunks, (u32)sm_count * 8), ITPB, 0, s>>>(a); }));
     KGB_CHECK(go(K_INV_RANKINIT, (u32)nchains, [&] { k_inv_rank_init<<<g4, 256, 0, s>>>(a); }));
     for (u32 j = 0; j < njump; j++) {
@@ -463,16 +492,17 @@ int InvEngine::run(cudaStream_t s, bool use_graph) {
     prof_run = !use_graph && prof.on;
     if (!use_graph) return enqueue(s, &stats.launches);
     prof_run = false;
-    const u64 key = ((u64)B << 40) ^ N ^ ((u64)(uintptr_t)d_U << 1) ^ ((u64)(uintptr_t)d_out << 3) ^ (ntiles << 17) ^
+    const u64 key = ((u64)B << 40) ^ N ^ ((u64)(uintptr_t)d_U << 1) ^ ((u64)(uintptr_t)d_out << 3) ^ (nchunk_all << 17) ^
                     (nchains << 23) ^ ((u64)njump << 58) ^ ((u64)nchunks << 29) ^ (Ncap << 11);
     if (!gexec || key != graph_key) {
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
-        KGB_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+        KGB_CHECK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
         long long dummy = 0;
-        int rc = enqueue(s, &dummy);
+        int rc = enqueue(cap_stream, &dummy);
         cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamEndCapture(s, &g);
+        cudaError_t e = cudaStreamEndCapture(cap_stream, &g);
         if (rc) { if (g) cudaGraphDestroy(g); return rc; }
         KGB_CHECK(e);
         graph = g;

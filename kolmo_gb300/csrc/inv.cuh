@@ -10,8 +10,8 @@ struct InvBlock {
     u32 off;         // first byte of the block's BWT string (and of its decoded text)
     u32 n;           // block length
     u32 p0;          // primary index (row of the sentinel in the L column), 1..n
-    u32 tile_base;   // first 4096-byte tile of the block
-    u32 ntiles;
+    u32 chunk_base;  // first 64 KiB chunk of the block (psi build)
+    u32 nchunk;
     u32 chain_base;  // first chain record of the block
     u32 nreg;        // regular marks (rows M, 2M, ..., nreg * M)
     u32 chain_cap;   // chain records reserved for the block
@@ -48,14 +48,14 @@ class InvEngine {
     void free_all();
     u64 Ncap = 0, Tcap = 0, Ccap = 0;
     u32 Bcap = 0;
-    u64 N = 0, ntiles = 0, nchains = 0;
+    u64 N = 0, nchunk_all = 0, nchains = 0;
     u32 B = 0, maxchains = 0, njump = 0, nchunks = 0;
     std::vector<u32> h_off;
     std::vector<InvBlock> h_blk;
     std::vector<u32> h_chunks;  // (block, first chain, end chain) triples for the walk
     bool ext = false;
     u8 *d_U = nullptr, *d_out = nullptr, *own_U = nullptr, *own_out = nullptr;
-    u32 *d_psi = nullptr, *d_thist = nullptr, *d_C = nullptr, *d_tblk = nullptr;
+    u32 *d_psi = nullptr, *d_csum = nullptr, *d_C = nullptr, *d_cblk = nullptr;
     u32 *d_len = nullptr, *d_succ = nullptr, *d_nx[2] = {nullptr, nullptr}, *d_dist[2] = {nullptr, nullptr};
     u32 *d_dyn = nullptr, *d_status = nullptr, *d_chunks = nullptr;
     u8 *d_buf = nullptr;
@@ -65,6 +65,7 @@ class InvEngine {
     int *h_status = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    cudaStream_t cap_stream = nullptr;
     u64 graph_key = 0;
     int sm_count = 0;
 };
