@@ -120,6 +120,19 @@ int32_t kgbwt_engine_profile(kgbwt_engine *e, int32_t enable);
 int32_t kgbwt_engine_profile_read(kgbwt_engine *e, kgbwt_prof *out, int32_t cap);
 const char *kgbwt_kernel_name(int32_t kernel);
 
+/* ---- allocation-free inverse --------------------------------------------------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device memory (an embedding host that owns
+ * every device allocation through its own pool, a plugin inside such a host, a process whose device footprint must
+ * not grow after start-up): the inverse BWT of one block with all scratch in a static device array inside this
+ * library, sized for n <= 262144 bytes (about 2.5 MB, held on every GPU that loads the library until exit).
+ * dU: the block's BWT string (sentinel removed, as the drop-in U), dT: the decoded text, both device buffers of n
+ * bytes; p0 = I[0]. Returns 0, -1 for bad arguments, n above the maximum, or a string that is not a valid BWT,
+ * -2 for a CUDA error. The call waits for its work on `stream` (a cudaStream_t, NULL = the legacy default stream).
+ * It calls no device allocator. Every call uses the same static array: calls that overlap on the GPU (from two
+ * host threads, or on two streams) race and corrupt each other. The first call on each device looks up the array's
+ * device address; make that first call before any stream capture. */
+int32_t kgbwt_unbwt_noalloc(const uint8_t *dU, uint8_t *dT, int32_t n, int32_t p0, void *stream);
+
 /* ---- misc --------------------------------------------------------------------------------------------------------- */
 const char *kgbwt_last_error(void); /* text of the last error on this thread ("" if none) */
 int32_t kgbwt_version(void);

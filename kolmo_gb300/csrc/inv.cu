@@ -22,6 +22,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+
+#include "kgbwt.h"
 
 namespace kgb {
 
@@ -522,3 +525,116 @@ int InvEngine::fetch_status(cudaStream_t s, std::vector<int> &status) {
 }
 
 }  // namespace kgb
+
+// ------------------------------------------------------------------------------------------------ allocation-free
+// Inverse BWT for callers that cannot allocate device memory: code that runs where cudaMalloc is not allowed or not
+// wanted (a host that owns every device allocation through its own pool, a plugin loaded into such a host, a
+// process that must not grow its device footprint after start-up). Its scratch is one file-scope device array
+// sized for one block of at most NOALLOC_MAX_N bytes; every GPU that loads this library holds that array
+// (about 2.5 MB) until the process exits. The caller passes device input and output buffers.
+namespace kgb {
+
+constexpr u32 NOALLOC_MAX_N = 1u << 18;  // 256 KiB
+constexpr u32 NA_CHUNKS = (NOALLOC_MAX_N + ITILE * CHUNKT - 1) / (ITILE * CHUNKT);
+constexpr u32 NA_NREG = NOALLOC_MAX_N / MARK;
+constexpr u32 NA_CHAINS = NA_NREG + 1 + NOALLOC_MAX_N / CAPC + 4;
+constexpr u32 NA_WALK = (NA_NREG + 1 + CHUNK - 1) / CHUNK;
+
+struct NoAllocScratch {
+    u32 psi[NOALLOC_MAX_N + 16];
+    u32 csum[NA_CHUNKS * 256];
+    u32 C[264];
+    u32 cblk[NA_CHUNKS];
+    u32 chunks[3 * NA_WALK];
+    InvBlock blk[1];
+    u32 len[NA_CHAINS], succ[NA_CHAINS], nx[2][NA_CHAINS], dist[2][NA_CHAINS];
+    u32 dyn[4], status[4];
+    u8 buf[(size_t)NA_CHAINS * CAPC];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Device address of the scratch array, looked up once per device (with that device current).
+static NoAllocScratch *noalloc_scratch(int *rc) {
+    static std::mutex mu;
+    static NoAllocScratch *addr[128] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { *rc = record_cuda_error(e, "cudaGetDevice", __FILE__, __LINE__); return nullptr; }
+    if (dev < 0 || dev >= 128) { record_error("device index out of range"); *rc = -2; return nullptr; }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) { *rc = record_cuda_error(e, "cudaGetSymbolAddress", __FILE__, __LINE__); return nullptr; }
+        addr[dev] = reinterpret_cast<NoAllocScratch *>(p);
+    }
+    *rc = 0;
+    return addr[dev];
+}
+
+static int unbwt_noalloc(const u8 *dU, u8 *dT, u32 n, u32 p0, cudaStream_t s) {
+    int rc = 0;
+    NoAllocScratch *S = noalloc_scratch(&rc);
+    if (!S) return rc;
+    // host-side tables on the stack: one block, its chunk map and its walk work items
+    InvBlock B;
+    B.off = 0; B.n = n; B.p0 = p0;
+    B.chunk_base = 0; B.nchunk = (n + ITILE * CHUNKT - 1) / (ITILE * CHUNKT);
+    B.nreg = n / MARK; B.chain_base = 0; B.chain_cap = B.nreg + 1 + n / CAPC + 4;
+    u32 cblk[NA_CHUNKS] = {0};
+    u32 chunks[3 * NA_WALK];
+    u32 nwalk = 0;
+    for (u32 c = 0; c < B.nreg + 1; c += CHUNK, nwalk++) {
+        chunks[3 * nwalk] = 0; chunks[3 * nwalk + 1] = c; chunks[3 * nwalk + 2] = std::min(B.nreg + 1, c + CHUNK);
+    }
+    u32 njump = 1;
+    while ((1ull << njump) < (u64)B.chain_cap + 1) njump++;
+    njump += 1;
+    KGB_CHECK(cudaMemcpyAsync(S->blk, &B, sizeof(B), cudaMemcpyHostToDevice, s));
+    KGB_CHECK(cudaMemcpyAsync(S->cblk, cblk, sizeof(u32) * B.nchunk, cudaMemcpyHostToDevice, s));
+    KGB_CHECK(cudaMemcpyAsync(S->chunks, chunks, sizeof(u32) * 3 * nwalk, cudaMemcpyHostToDevice, s));
+    // the array keeps the previous call's contents: reset what must start at zero (or at "no successor")
+    KGB_CHECK(cudaMemsetAsync(S->len, 0, sizeof(u32) * B.chain_cap, s));
+    KGB_CHECK(cudaMemsetAsync(S->succ, 0xFF, sizeof(u32) * B.chain_cap, s));
+    KGB_CHECK(cudaMemsetAsync(S->dyn, 0, sizeof(S->dyn), s));
+    KGB_CHECK(cudaMemsetAsync(S->status, 0, sizeof(S->status), s));
+    InvArgs a;
+    memset(&a, 0, sizeof(a));
+    a.U = dU; a.out = dT; a.psi = S->psi; a.csum = S->csum; a.cblk = S->cblk; a.C = S->C; a.blk = S->blk; a.B = 1;
+    a.nchunk_all = B.nchunk; a.nchains = B.chain_cap; a.len = S->len; a.succ = S->succ; a.dyn = S->dyn;
+    a.status = S->status; a.nx[0] = S->nx[0]; a.nx[1] = S->nx[1]; a.dist[0] = S->dist[0]; a.dist[1] = S->dist[1];
+    a.buf = S->buf; a.chunks = S->chunks; a.nchunks = nwalk; a.jpar = 0; a.cap_n = n;
+    k_inv_chunkhist<<<B.nchunk, ITPB, 0, s>>>(a);
+    k_inv_chunkscan<<<1, ITPB, 0, s>>>(a);
+    k_inv_scatter<<<B.nchunk, ITPB, 0, s>>>(a);
+    k_inv_walk<<<nwalk, ITPB, 0, s>>>(a);
+    const int g = (int)((B.chain_cap + 255) / 256);
+    k_inv_rank_init<<<g, 256, 0, s>>>(a);
+    for (u32 j = 0; j < njump; j++) {
+        a.jpar = j & 1;
+        k_inv_jump<<<g, 256, 0, s>>>(a);
+    }
+    a.jpar = njump & 1;
+    k_inv_emit<<<(int)std::min<u32>(1024u, (B.chain_cap + 7) / 8), 256, 0, s>>>(a);
+    KGB_CHECK(cudaGetLastError());
+    u32 status = 0;
+    KGB_CHECK(cudaMemcpyAsync(&status, S->status, sizeof(u32), cudaMemcpyDeviceToHost, s));
+    KGB_CHECK(cudaStreamSynchronize(s));
+    if (status) { record_error("inverse BWT: not a valid BWT string for its primary index"); return -1; }
+    return 0;
+}
+
+}  // namespace kgb
+
+extern "C" int32_t kgbwt_unbwt_noalloc(const uint8_t *dU, uint8_t *dT, int32_t n, int32_t p0, void *stream) {
+    if (!dU || !dT || n < 2 || p0 < 1 || p0 > n) {
+        kgb::record_error("kgbwt_unbwt_noalloc: bad arguments (device buffers, n >= 2, 1 <= p0 <= n)");
+        return -1;
+    }
+    if ((uint32_t)n > kgb::NOALLOC_MAX_N) {
+        kgb::record_error("kgbwt_unbwt_noalloc: n exceeds the maximum of 262144 bytes of the static scratch");
+        return -1;
+    }
+    return kgb::unbwt_noalloc(dU, dT, (kgb::u32)n, (kgb::u32)p0, (cudaStream_t)stream);
+}

@@ -87,6 +87,8 @@ def lib():
     L.kgbwt_engine_profile_read.restype = _I32
     L.kgbwt_kernel_name.argtypes = [_I32]
     L.kgbwt_kernel_name.restype = ctypes.c_char_p
+    L.kgbwt_unbwt_noalloc.argtypes = [_P, _P, _I32, _I32, _P]
+    L.kgbwt_unbwt_noalloc.restype = _I32
     L.kgbwt_last_error.restype = ctypes.c_char_p
     L.kgbwt_version.restype = _I32
     _lib = L
@@ -103,4 +105,5 @@ EXPORTS = (
     "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
     "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
     "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_small_group",
+    "kgbwt_unbwt_noalloc",
 )
