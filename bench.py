@@ -190,9 +190,9 @@ def algorithmic_bytes(rec: dict) -> float:
     round 0 33 B per suffix, the inverse 10 B per byte over its passes (psi build: read L, write psi; walk: read psi,
     write text)."""
     k, e = rec["kernel"], rec["elems"]
-    if k in ("tile_sort_rank", "tile_sort_rank_keyed"):
+    if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed"):
         return 48.0 * e
-    if k in ("tile_sort_prefix", "tile_sort_prefix_keyed"):
+    if k in ("tile_sort_prefix", "tile_sort_prefix_keyed", "tile_warp_prefix", "tile_warp_prefix_keyed"):
         return 33.0 * e
     if k == "inv_walk":
         return 5.0 * e   # read psi 4 B + write 1 B per decoded byte
@@ -221,7 +221,7 @@ def run_ours(args, world, rank, local):
     ns = n_samples(n, r)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
-    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group)
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path)
     dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
     dT[:n] = torch.from_numpy(T).to(dev)
     dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
@@ -282,7 +282,7 @@ def run_ours(args, world, rank, local):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
                 "fwd_ms": round(sum(tf) / len(tf), 3), "inv_ms": round(sum(ti) / len(ti), 3),
                 "block_bytes": n, "skip_extras": True,
-                "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group]}
+                "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path]}
 
     # profiled pass (plain path, CUDA events around every launch on stream s)
     eng.profile(True)
@@ -292,6 +292,9 @@ def run_ours(args, world, rank, local):
     assert eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True) == 0 and eng.wait(1)[0] == 0
     prof_i = eng.profile_read()
     eng.profile(False)
+    if args.profile_out and rank == 0:
+        with open(args.profile_out, "w") as f:
+            json.dump({"forward": prof_f, "inverse": prof_i}, f)
     launches_fwd = sum(1 for x in prof_f)
     launches_inv = sum(1 for x in prof_i)
     prof = prof_f + prof_i
@@ -310,7 +313,7 @@ def run_ours(args, world, rank, local):
     for rec in prof_f:
         rr = rounds.setdefault(rec["round"], {"ms": 0.0, "m": 0})
         rr["ms"] += rec["ms"]
-        if rec["kernel"] in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_sort_prefix", "tile_sort_prefix_keyed"):
+        if rec["kernel"].startswith(("tile_sort", "tile_warp")):
             rr["m"] += rec["elems"]
     round_table = []
     for j in sorted(rounds):
@@ -441,6 +444,8 @@ def main():
     ap.add_argument("--tile-ctas", type=int, default=0)
     ap.add_argument("--msd-ctas", type=int, default=0)
     ap.add_argument("--small-group", type=int, default=-1)
+    ap.add_argument("--warp-path", type=int, default=-1)
+    ap.add_argument("--profile-out", default="", help="write the per-launch profile of the profiled step here")
     ap.add_argument("--plain", action="store_true",
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")
     ap.add_argument("--skip-extras", action="store_true",

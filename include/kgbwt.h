@@ -85,9 +85,13 @@ void kgbwt_engine_destroy(kgbwt_engine *e);
 /* tile_cap 4096 or 8192 (largest group sorted in one tile = tile_cap / 2); tile_ctas, msd_ctas: persistent CTAs
  * per SM of the tile sorter and of the bucket passes. 0 keeps the current value. Returns 0 or -1. */
 int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas, int32_t msd_ctas);
-/* Tiles whose groups are all at most small_group long are sorted by counting inside each group instead of radix
- * passes (0..1024; 0 disables). Results never depend on it. Returns 0 or -1. */
-int32_t kgbwt_engine_small_group(kgbwt_engine *e, int32_t small_group);
+/* Tuning options (results never depend on them). Returns 0 or -1 for an unknown option or value.
+ * KGBWT_OPT_SMALL_GROUP (0..1024, default 64): tiles whose groups are all at most this long are sorted by counting
+ *   inside each group instead of radix passes (0: always radix).
+ * KGBWT_OPT_WARP_PATH (0/1, default 1): tiles whose groups are all at most 32 long go to the warp-level kernel. */
+#define KGBWT_OPT_SMALL_GROUP 1
+#define KGBWT_OPT_WARP_PATH 2
+int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value);
 /* Forward: text blocks in dT (16 readable bytes past the last block). Results: dL receives each block's L column
  * with its sentinel row (n + 1 bytes at off + block index; row p0 holds no text byte), dI the sampled indexes at
  * iout (dI[iout] = primary index), dSA (may be NULL) the suffix array at off. */

@@ -103,12 +103,16 @@ class Engine:
         if tile_cap or tile_ctas or msd_ctas:
             self.config(tile_cap, tile_ctas, msd_ctas)
 
-    def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1):
-        rc = native.lib().kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
+    def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1,
+               warp_path: int = -1):
+        L = native.lib()
+        rc = L.kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
         if rc == 0 and small_group >= 0:
-            rc = native.lib().kgbwt_engine_small_group(self.h, small_group)
+            rc = L.kgbwt_engine_option(self.h, native.OPT_SMALL_GROUP, small_group)
+        if rc == 0 and warp_path >= 0:
+            rc = L.kgbwt_engine_option(self.h, native.OPT_WARP_PATH, warp_path)
         if rc:
-            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group}")
+            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group} {warp_path}")
 
     def close(self):
         if self.h:

@@ -19,6 +19,7 @@ const char *kernel_name(int k) {
     static const char *names[K_NKERNELS] = {
         "init", "fixup", "keygen", "msd_hist", "msd_scan", "msd_scatter", "tile_sort_prefix", "tile_sort_prefix_keyed",
         "tile_sort_rank", "tile_sort_rank_keyed", "control", "samples",
+        "tile_warp_prefix", "tile_warp_prefix_keyed", "tile_warp_rank", "tile_warp_rank_keyed",
         "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
@@ -264,11 +265,21 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
     return 0;
 }
 
-int32_t kgbwt_engine_small_group(kgbwt_engine *e, int32_t small_group) {
-    if (!e || small_group < 0 || small_group > 1024) return -1;
+int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
+    if (!e) return -1;
     std::lock_guard<std::mutex> lock(e->mu);
-    e->fwd.cfg.small_group = small_group;
-    return 0;
+    switch (option) {
+        case KGBWT_OPT_SMALL_GROUP:
+            if (value < 0 || value > 1024) return -1;
+            e->fwd.cfg.small_group = value;
+            return 0;
+        case KGBWT_OPT_WARP_PATH:
+            if (value != 0 && value != 1) return -1;
+            e->fwd.cfg.warp_path = value;
+            return 0;
+        default:
+            return -1;
+    }
 }
 
 int32_t kgbwt_engine_fwd(kgbwt_engine *e, const uint8_t *dT, uint8_t *dL, int32_t *dI, int32_t *dSA,

@@ -36,6 +36,11 @@ constexpr int TPB = 256;
 constexpr int TSM = 2048;  // elements per tile of the bucket passes
 constexpr int IPM = TSM / TPB;
 constexpr u32 DEPTH_PREFIX = 8, DEPTH_RANK = 4;
+constexpr u32 WARP_GROUP = 32;  // groups up to this long are handled by one warp (k_tile_warp)
+// Seg.bd flag of small groups: the group came from the previous round's small-group list and passed that round
+// unsplit, so both rank buffers already hold its head (set only on groups whose input was a small-group list: a group
+// cut out of a larger one by the bucket passes has its parent's head in the other buffer).
+constexpr u32 STABLE = 0x80000000u;
 
 enum : u8 { C_NONE = 0, C_KS = 1, C_KO = 2, C_LN = 3, C_ONE = 4 };
 
@@ -49,10 +54,12 @@ struct FwdArgs {
     u32 *I;
     ListView lists[NLISTS];
     u32 *hist, *cursor, *bhead, *orand;
+    u64 *orand64;  // prefix rounds: OR and AND of each bucket-pass group's 8-byte prefixes
     u8 *dest;
     u32 B;
     u32 smax;
     u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
+    u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segl, cap_tms, cap_tml;
@@ -164,6 +171,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             continue;
         }
         if (sa_ >= sb_) continue;
+        if (a.warp_path && in.tbig[t] != ctl->round) continue;  // all groups short: the warp kernel's tile
         const u32 nsegs = sb_ - sa_;
         const u32 E0 = in.seg[sa_].start;
         const u32 E1 = sb_ < nseg ? in.seg[sb_].start : nelem;
@@ -175,8 +183,8 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
         for (u32 j = tid; j < nsegs; j += TPB) {
             Seg g = in.seg[sa_ + j];
             S.lstart[j] = g.start - E0;
-            S.lhead[j] = g.head;
-            S.lblk[j] = seg_blk(g.bd);
+            S.lhead[j] = g.head;  // bit 31 is set below when the group splits
+            S.lblk[j] = g.bd;     // block | STABLE
         }
         if (tid == 0) S.lstart[nsegs] = cnt;
         __syncthreads();
@@ -198,7 +206,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 }
                 KeyT key;
                 if (PREFIX) {
-                    const BlockInfo B = a.blk[S.lblk[lo]];
+                    const BlockInfo B = a.blk[seg_blk(S.lblk[lo])];
                     const u64 end = (u64)B.off + B.n;
                     u64 kk = load_be64(a.T, id);
                     const u64 rem = end - id;
@@ -207,7 +215,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 } else if (KEYED) {
                     key = in.ekey[E0 + x];
                 } else {
-                    const BlockInfo B = a.blk[S.lblk[lo]];
+                    const BlockInfo B = a.blk[seg_blk(S.lblk[lo])];
                     key = rank_key(isa_cur, id, h, (u64)B.off + B.n);
                 }
                 k[j] = key;
@@ -344,6 +352,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 st[j] = x == S.lstart[sj] || kx != S.klo[x - 1];
                 en[j] = x + 1 == S.lstart[sj + 1] || kx != S.klo[x + 1];
                 if (st[j]) gl = x;
+                if (st[j] && x != S.lstart[sj]) atomicOr(&S.lhead[sj], 0x80000000u);  // the group splits
                 const u32 surv = !(st[j] && en[j]);
                 ns += surv;
                 ng += surv && st[j];
@@ -365,6 +374,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
         const u32 pre = block_excl_sum<TPB>(ns | (ng << 16), S.ws, &tot_pack);
         const u32 tot_s = tot_pack & 0xFFFFu, tot_g = tot_pack >> 16;
         if (tid == 0) {
+            atomicAdd(&a.ctl->tile_elems[0], (u64)cnt);
             const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)tot_g << 32) | tot_s);
             S.bases[0] = (u32)o;
             S.bases[1] = (u32)(o >> 32);
@@ -381,24 +391,264 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             if (st[j]) gfirst = x;
             const u32 sj = S.khi[x], id = S.val[x];
             const u32 s0 = S.lstart[sj];
+            const u32 lh = S.lhead[sj], bd = S.lblk[sj];
+            const bool unsplit = !(lh >> 31);
             if (st[j] && en[j]) {
-                resolve(a, isa_nxt, id, S.lhead[sj] + (x - s0), S.lblk[sj], res, rbase + (x - es));
+                resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + (x - es));
             } else {
-                const u32 head = S.lhead[sj] + (gfirst - s0);
-                KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+                const u32 head = (lh & 0x7FFFFFFFu) + (gfirst - s0);
+                // a group that passed the previous round unsplit and passes this one unsplit already has this head
+                // in the write buffer (written two rounds ago)
+                if (!((bd & STABLE) && unsplit)) {
+                    KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+                }
                 KGB_GUARD(ebase + es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + es] = id;
                 if (st[j]) gs++;
                 if (en[j]) {
                     const u32 len = x - gfirst + 1, sidx = sbase + gs - 1, start = ebase + es + 1 - len;
                     Seg g;
-                    g.start = start; g.len = len; g.head = head; g.bd = S.lblk[sj];
+                    g.start = start; g.len = len; g.head = head;
+                    g.bd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
                     KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
                     write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                    if (len > WARP_GROUP) out.tbig[start / TS] = ctl->round + 1;
                 }
                 es++;
             }
         }
         __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------ warp tiles
+// Tiles whose groups are all at most WARP_GROUP long (no stamp in tbig for this round). The CTA loads the tile's
+// segment descriptors once; then each warp independently takes the groups starting in one eighth of the tile window:
+// it gathers their keys into shared memory, sorts every group by counting (a group fits in one warp), and emits
+// ranks, finished suffixes and surviving groups with warp scans and one allocation atomic per warp. No block-wide
+// barrier after the descriptor load.
+
+template <int TILE, typename KeyT>
+struct WarpSmem {
+    static constexpr int TS = TILE / 2;
+    static constexpr int CAPE = TS + WARP_GROUP;  // at most TS + WARP_GROUP - 1 elements in a window
+    u32 lstart[TS + 1];
+    u32 lhead[TS];
+    u32 lbd[TS];
+    KeyT key[2][CAPE];  // gathered order, then sorted order
+    u32 val[2][CAPE];
+    u16 sg[2][CAPE];
+};
+
+template <bool PREFIX, bool KEYED, int TILE>
+__global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
+    typedef typename TileTraits<PREFIX, TILE>::KeyT KeyT;
+    constexpr int TS = TILE / 2, NW = TPB / 32, SW = TS / NW, PER = (SW + WARP_GROUP + 31) / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WarpSmem<TILE, KeyT> &S = *reinterpret_cast<WarpSmem<TILE, KeyT> *>(smem_raw);
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h, round = ctl->round;
+    const u32 lin = KEYED ? L_KS : L_S0 + rpar;
+    const ListView in = a.lists[lin];
+    const ListView out = a.lists[L_S0 + (rpar ^ 1)];
+    const ListView res = a.lists[L_R0 + rpar];
+    const u64 c = ctl->cnt[lin];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segs) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 ntiles = (u32)(((u64)nelem + TS - 1) / TS);
+    const u32 *isa_cur = a.isa[rpar];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 lane = lane_id(), warp = warp_id(), tid = threadIdx.x;
+    const u32 lt_mask = lanemask_lt();
+
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const u32 sa_ = in.tmap[t];
+        const u32 sb_ = t + 1 < ntiles ? in.tmap[t + 1] : nseg;
+        if (sa_ > nseg || sb_ > nseg) {
+            if (tid == 0) atomicOr(&a.ctl->err, E_TMAP);
+            continue;
+        }
+        if (sa_ >= sb_ || in.tbig[t] == round) continue;  // empty, or a block-kernel tile
+        const u32 nsegs = sb_ - sa_;
+        const u32 E0 = in.seg[sa_].start;
+        const u32 E1 = sb_ < nseg ? in.seg[sb_].start : nelem;
+        const u32 cnt = E1 - E0;
+        if (nsegs > (u32)TS || E1 < E0 || cnt > (u32)(TS + WARP_GROUP) || E1 > nelem) {
+            if (tid == 0) atomicOr(&a.ctl->err, E_TILE);
+            continue;
+        }
+        __syncthreads();  // the previous tile's warps are done with the descriptors
+        for (u32 j = tid; j < nsegs; j += TPB) {
+            const Seg g = in.seg[sa_ + j];
+            S.lstart[j] = g.start - E0;
+            S.lhead[j] = g.head;
+            S.lbd[j] = g.bd;
+        }
+        if (tid == 0) S.lstart[nsegs] = cnt;
+        __syncthreads();
+
+        // this warp's groups: those starting in [t*TS + warp*SW, t*TS + (warp+1)*SW) of the list
+        auto first_at = [&](u64 pos) -> u32 {  // first segment with list start >= pos
+            if (pos <= E0) return 0;
+            const u32 lp = (u32)(pos - E0);
+            u32 lo = 0, hi = nsegs;
+            while (lo < hi) {
+                const u32 mid = (lo + hi) >> 1;
+                if (S.lstart[mid] < lp) lo = mid + 1; else hi = mid;
+            }
+            return lo;
+        };
+        const u64 w0 = (u64)t * TS + (u64)warp * SW;
+        const u32 j0 = first_at(w0);
+        const u32 j1 = warp + 1 == NW ? nsegs : first_at(w0 + SW);
+        if (j0 >= j1) continue;
+        const u32 X0 = S.lstart[j0], X1 = S.lstart[j1];
+        if (X1 - X0 > (u32)PER * 32) {  // a long group reached a warp tile: report, never overrun
+            if (lane == 0) atomicOr(&a.ctl->err, E_TILE);
+            continue;
+        }
+
+        // ---- gather keys (4 loads in flight per lane) into buffer 0
+        for (u32 xb = X0; xb < X1; xb += 128) {
+            u32 ids[4], sgs[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const u32 x = xb + q * 32 + lane;
+                ids[q] = x < X1 ? in.eid[E0 + x] : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const u32 x = xb + q * 32 + lane;
+                u32 lo = j0, hi = j1 - 1;  // last segment with lstart <= x
+                while (lo < hi) {
+                    const u32 mid = (lo + hi + 1) >> 1;
+                    if (S.lstart[mid] <= x) lo = mid; else hi = mid - 1;
+                }
+                sgs[q] = lo;
+            }
+            KeyT keys[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const u32 x = xb + q * 32 + lane;
+                keys[q] = 0;
+                if (x < X1) {
+                    if (KEYED && !PREFIX) {
+                        keys[q] = in.ekey[E0 + x];
+                    } else {
+                        const BlockInfo B = a.blk[seg_blk(S.lbd[sgs[q]])];
+                        const u64 end = (u64)B.off + B.n;
+                        if (PREFIX) {
+                            u64 kk = load_be64(a.T, ids[q]);
+                            const u64 rem = end - ids[q];
+                            if (rem < 8) kk &= ~0ull << (8 * (8 - rem));
+                            keys[q] = (KeyT)kk;
+                        } else {
+                            keys[q] = (KeyT)rank_key(isa_cur, ids[q], h, end);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const u32 x = xb + q * 32 + lane;
+                if (x < X1) { S.key[0][x] = keys[q]; S.val[0][x] = ids[q]; S.sg[0][x] = (u16)sgs[q]; }
+            }
+        }
+        __syncwarp();
+        // ---- sort each group by counting into buffer 1 (position = keys below + equal keys before); lanes of a
+        // long group read the same key at each step (shared-memory broadcast)
+        for (u32 x = X0 + lane; x < X1; x += 32) {
+            const u32 sj = S.sg[0][x];
+            const u32 g0 = S.lstart[sj], g1 = S.lstart[sj + 1];
+            const KeyT kx = S.key[0][x];
+            u32 below = 0;
+            for (u32 y = g0; y < g1; y++) {
+                const KeyT ky = S.key[0][y];
+                below += ky < kx || (ky == kx && y < x);
+            }
+            const u32 d = g0 + below;
+            S.key[1][d] = kx; S.val[1][d] = S.val[0][x]; S.sg[1][d] = (u16)sj;
+        }
+        __syncwarp();
+        // ---- count survivors, groups, finished suffixes; mark segments that split
+        u32 ns = 0, ng = 0;
+        for (u32 xb = X0; xb < X1; xb += 32) {
+            const u32 x = xb + lane;
+            bool st = false, en = false;
+            if (x < X1) {
+                const u32 sj = S.sg[1][x];
+                const KeyT kx = S.key[1][x];
+                st = x == S.lstart[sj] || kx != S.key[1][x - 1];
+                en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
+                if (st && x != S.lstart[sj]) atomicOr(&S.lhead[sj], 0x80000000u);
+            }
+            const bool surv = x < X1 && !(st && en);
+            ns += __popc(__ballot_sync(0xffffffffu, surv));
+            ng += __popc(__ballot_sync(0xffffffffu, surv && st));
+        }
+        const u32 nres = (X1 - X0) - ns;
+        u32 ebase = 0, sbase = 0, rbase = 0;
+        if (lane == 0) {
+            atomicAdd(&a.ctl->tile_elems[1], (u64)(X1 - X0));
+            if (ns) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)ng << 32) | ns);
+                ebase = (u32)o; sbase = (u32)(o >> 32);
+            }
+            if (nres) rbase = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)nres);
+        }
+        ebase = __shfl_sync(0xffffffffu, ebase, 0);
+        sbase = __shfl_sync(0xffffffffu, sbase, 0);
+        rbase = __shfl_sync(0xffffffffu, rbase, 0);
+        __syncwarp();
+        // ---- emit
+        u32 es = 0, gs = 0, rs = 0, carry = X0;  // running counts; carry: start of the open group
+        for (u32 xb = X0; xb < X1; xb += 32) {
+            const u32 x = xb + lane;
+            const bool valid = x < X1;
+            bool st = false, en = false;
+            u32 sj = 0;
+            if (valid) {
+                sj = S.sg[1][x];
+                const KeyT kx = S.key[1][x];
+                st = x == S.lstart[sj] || kx != S.key[1][x - 1];
+                en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
+            }
+            const bool single = valid && st && en, surv = valid && !(st && en);
+            const u32 b_surv = __ballot_sync(0xffffffffu, surv), b_gs = __ballot_sync(0xffffffffu, surv && st);
+            const u32 b_one = __ballot_sync(0xffffffffu, single);
+            const u32 gf = warp_incl_max(valid && st ? x : 0u);
+            const u32 gfirst = max(gf, carry);
+            const u32 my_es = es + __popc(b_surv & lt_mask), my_gs = gs + __popc(b_gs & lt_mask);
+            const u32 my_rs = rs + __popc(b_one & lt_mask);
+            if (valid) {
+                const u32 id = S.val[1][x], s0 = S.lstart[sj], lh = S.lhead[sj], bd = S.lbd[sj];
+                const bool unsplit = !(lh >> 31);
+                if (single) {
+                    resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + my_rs);
+                } else {
+                    const u32 head = (lh & 0x7FFFFFFFu) + (gfirst - s0);
+                    if (!((bd & STABLE) && unsplit)) {
+                        KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+                    }
+                    KGB_GUARD(ebase + my_es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + my_es] = id;
+                    if (en) {
+                        const u32 len = x - gfirst + 1, sidx = sbase + my_gs + (st ? 1u : 0u) - 1u;
+                        const u32 start = ebase + my_es + 1 - len;
+                        Seg g;
+                        g.start = start; g.len = len; g.head = head;
+                        g.bd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
+                        KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
+                        write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                    }
+                }
+            }
+            es += __popc(b_surv);
+            gs += __popc(b_gs);
+            rs += __popc(b_one);
+            carry = __shfl_sync(0xffffffffu, gfirst, 31);
+        }
     }
 }
 
@@ -515,6 +765,7 @@ __global__ void __launch_bounds__(TPB) k_msd_hist(FwdArgs a) {
         MsdTile m;
         msd_tile_info<PREFIX>(a, in, nseg, t, pass == 0, m);
         __syncthreads();
+        u64 or0 = 0, and0 = ~0ull, or1 = 0, and1 = ~0ull;  // prefix rounds: which prefix bytes vary per group
 #pragma unroll
         for (int j = 0; j < IPM; j++) {
             const u32 x = t * TSM + j * TPB + threadIdx.x;
@@ -522,12 +773,39 @@ __global__ void __launch_bounds__(TPB) k_msd_hist(FwdArgs a) {
             u32 kk = 0xFFFFFFFFu;
             if (valid) {
                 const bool sel = x >= m.bound;
-                u32 key;
-                const u32 d = msd_digit<PREFIX>(a, in, x, in.eid[x], sel ? m.g1 : m.g0, sel ? m.d1 : m.d0, &key);
+                const u32 id = in.eid[x];
+                u32 d;
+                if (PREFIX) {
+                    const BlockInfo B = a.blk[seg_blk((sel ? m.g1 : m.g0).bd)];
+                    u64 pk = load_be64(a.T, id);
+                    const u64 rem = (u64)B.off + B.n - id;
+                    if (rem < 8) pk &= ~0ull << (8 * (8 - rem));
+                    d = (u32)(pk >> (56 - 8 * (sel ? m.d1 : m.d0))) & 0xFF;
+                    if (sel) { or1 |= pk; and1 &= pk; } else { or0 |= pk; and0 &= pk; }
+                } else {
+                    u32 key;
+                    d = msd_digit<PREFIX>(a, in, x, id, sel ? m.g1 : m.g0, sel ? m.d1 : m.d0, &key);
+                }
                 kk = ((u32)sel << 8) | d;
             }
             const u32 peers = __match_any_sync(0xffffffffu, kk);
             if (valid && (__ffs(peers) - 1) == (int)lane) atomicAdd(&(&hs[0][0])[kk], __popc(peers));
+        }
+        if (PREFIX) {
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                or0 |= __shfl_xor_sync(0xffffffffu, or0, o);
+                and0 &= __shfl_xor_sync(0xffffffffu, and0, o);
+                or1 |= __shfl_xor_sync(0xffffffffu, or1, o);
+                and1 &= __shfl_xor_sync(0xffffffffu, and1, o);
+            }
+            if (lane == 0) {
+                if (or0 || and0 != ~0ull) { atomicOr(&a.orand64[2 * m.s0], or0); atomicAnd(&a.orand64[2 * m.s0 + 1], and0); }
+                if (m.s1 != m.s0 && (or1 || and1 != ~0ull)) {
+                    atomicOr(&a.orand64[2 * m.s1], or1);
+                    atomicAnd(&a.orand64[2 * m.s1 + 1], and1);
+                }
+            }
         }
         __syncthreads();
         for (int i = threadIdx.x; i < 512; i += TPB) {
@@ -574,7 +852,13 @@ __global__ void __launch_bounds__(TPB) k_msd_scan(FwdArgs a) {
         const u32 cc = a.hist[hrow + tid];
         a.hist[hrow + tid] = 0;
         const u32 excl = block_excl_sum<TPB>(cc, S.ws, nullptr);
-        const u32 nd = d + 1, maxd = PREFIX ? DEPTH_PREFIX : DEPTH_RANK;
+        u32 nd = d + 1;
+        const u32 maxd = PREFIX ? DEPTH_PREFIX : DEPTH_RANK;
+        if (PREFIX) {
+            // the next depth skips prefix bytes that are the same in the whole group (all of them: the group is final)
+            const u64 vary = a.orand64[2 * s] ^ a.orand64[2 * s + 1];
+            while (nd < DEPTH_PREFIX && !((vary >> (56 - 8 * nd)) & 0xFF)) nd++;
+        }
         u8 cls = cc == 0 ? C_NONE : cc == 1 ? C_ONE : cc <= a.smax ? C_KS : nd >= maxd ? C_LN : C_KO;
         // element and segment counts per class (singletons need only a resolved-list slot)
         u32 e_ks = cls == C_KS ? cc : 0, e_ko = cls == C_KO ? cc : 0, e_ln = cls == C_LN ? cc : 0;
@@ -611,6 +895,7 @@ __global__ void __launch_bounds__(TPB) k_msd_scan(FwdArgs a) {
             a.cursor[hrow + tid] = start;
             if (cls == C_KS) {
                 write_tmap_small(a, o.tmap, a.smax, start, cc, sidx);
+                if (cc > WARP_GROUP) o.tbig[start / a.smax] = ctl->round;
             } else {
                 t0 = (start + TSM - 1) / TSM;
                 const u32 t1 = (u32)(((u64)start + cc - 1) / TSM);
@@ -619,6 +904,8 @@ __global__ void __launch_bounds__(TPB) k_msd_scan(FwdArgs a) {
         }
         a.bhead[hrow + tid] = head;
         a.dest[hrow + tid] = cls;
+        __syncthreads();  // every thread has read orand64[s]
+        if (PREFIX && tid == 0) { a.orand64[2 * s] = 0; a.orand64[2 * s + 1] = ~0ull; }
         if (!PREFIX && pass == 0 && tid == 0) {  // the scatter reads the digit from the descriptor
             a.orand[2 * s] = 0;
             a.orand[2 * s + 1] = ~0u;
@@ -854,6 +1141,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
         if (!res) {
             add((void **)&lists[l].seg, (small ? nseg_small : nseg_large) * sizeof(Seg));
             add((void **)&lists[l].tmap, (small ? ntm_small : ntm_large) * 4);
+            if (small) add((void **)&lists[l].tbig, ntm_small * 4);
         }
     }
     add((void **)&d_hist, nseg_large * 256 * 4);
@@ -861,6 +1149,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     add((void **)&d_bhead, nseg_large * 256 * 4);
     add((void **)&d_dest, nseg_large * 256);
     add((void **)&d_orand, nseg_large * 8);
+    add((void **)&d_orand64, nseg_large * 16);
     add((void **)&d_ctl, sizeof(Ctl));
     size_t total = 0;
     for (auto &it : items) total += it.bytes;
@@ -875,11 +1164,15 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     size_t off = 0;
     for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
+    for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemset(lists[l].tbig, 0xFF, ntm_small * 4));
     // orand rows start as (or = 0, and = ~0)
     {
         std::vector<u32> init(2 * nseg_large);
         for (size_t i = 0; i < nseg_large; i++) { init[2 * i] = 0; init[2 * i + 1] = ~0u; }
         KGB_CHECK(cudaMemcpy(d_orand, init.data(), init.size() * 4, cudaMemcpyHostToDevice));
+        std::vector<u64> init64(2 * nseg_large);
+        for (size_t i = 0; i < nseg_large; i++) { init64[2 * i] = 0; init64[2 * i + 1] = ~0ull; }
+        KGB_CHECK(cudaMemcpy(d_orand64, init64.data(), init64.size() * 8, cudaMemcpyHostToDevice));
     }
     if (!h_ctl) KGB_CHECK(cudaMallocHost(&h_ctl, sizeof(Ctl)));
     Ncap = ncap;
@@ -891,7 +1184,9 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 }
 
 void FwdEngine::set_caps(FwdArgs &a) const {
+    a.orand64 = d_orand64;
     a.small_group = (u32)cfg.small_group;
+    a.warp_path = (u32)cfg.warp_path;
     a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_tms = cap_tms; a.cap_tml = cap_tml;
 }
 
@@ -948,7 +1243,7 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     std::vector<u32> lstart(B);
     std::vector<u8> large(B);
     std::vector<Seg> seg_s, seg_l;
-    std::vector<u32> tm_s, tm_l;
+    std::vector<u32> tm_s, tm_l, big_s;
     u64 es = 0, el = 0;
     for (u32 b = 0; b < B; b++) {
         bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b]};
@@ -964,6 +1259,7 @@ int FwdEngine::setup_round0(cudaStream_t s) {
             g.start = (u32)es; lstart[b] = (u32)es;
             u64 t = (es + smax - 1) / smax;
             if (t * smax < es + h_n[b]) { if (tm_s.size() <= t) tm_s.resize(t + 1); tm_s[t] = (u32)seg_s.size() + (t * smax == es ? 0 : 1); }
+            if (h_n[b] > WARP_GROUP) big_s.push_back((u32)(es / smax));
             seg_s.push_back(g);
             es += h_n[b];
         }
@@ -975,9 +1271,16 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     c.cnt[L_L0] = ((u64)seg_l.size() << 32) | el;
     c.maxrounds = (u32)ceil_log2(maxn) + 3;
     KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
+    const size_t ntm = cap_tms;
+    for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemsetAsync(lists[l].tbig, 0xFF, ntm * 4, s));
     if (!seg_s.empty()) {
         KGB_CHECK(cudaMemcpyAsync(lists[L_S0].seg, seg_s.data(), seg_s.size() * sizeof(Seg), cudaMemcpyHostToDevice, s));
         if (!tm_s.empty()) KGB_CHECK(cudaMemcpyAsync(lists[L_S0].tmap, tm_s.data(), tm_s.size() * 4, cudaMemcpyHostToDevice, s));
+        // round-0 stamps (value 0) of windows where a block longer than WARP_GROUP starts
+        std::vector<u32> stamp(tm_s.size() + 1, 0xFFFFFFFFu);
+        for (u32 t : big_s) if (t < stamp.size()) stamp[t] = 0;
+        KGB_CHECK(cudaMemcpyAsync(lists[L_S0].tbig, stamp.data(), stamp.size() * 4, cudaMemcpyHostToDevice, s));
+        KGB_CHECK(cudaStreamSynchronize(s));  // `stamp` is a local
     }
     if (!seg_l.empty()) {
         KGB_CHECK(cudaMemcpyAsync(lists[L_L0].seg, seg_l.data(), seg_l.size() * sizeof(Seg), cudaMemcpyHostToDevice, s));
@@ -1004,16 +1307,19 @@ static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const
     a.ctl = ctl; a.T = T; a.blk = blk; a.isa[0] = isa[0]; a.isa[1] = isa[1]; a.L = L; a.SA = SA; a.I = I;
     for (int l = 0; l < NLISTS; l++) a.lists[l] = lists[l];
     a.hist = hist; a.cursor = cursor; a.bhead = bhead; a.orand = orand; a.dest = dest; a.B = B; a.smax = smax;
+    a.orand64 = nullptr;
     a.hcond = 0;
     return a;
 }
 
 template <bool PREFIX, int TILE>
 static int tile_smem() { return (int)sizeof(TileSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
+template <bool PREFIX, int TILE>
+static int warp_smem() { return (int)sizeof(WarpSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
 
 struct Launcher {
     cudaStream_t s;
-    int grid_tile, grid_msd, grid_scan, tile_cap, grid_tile_prefix;
+    int grid_tile, grid_msd, grid_scan, tile_cap, grid_tile_prefix, grid_warp;
     long long *launches;
     Profiler *prof;
     template <typename K, typename... Args>
@@ -1043,12 +1349,53 @@ static int set_tile_attrs(int tile) {
         KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 8192>()));
         KGB_CHECK(cudaFuncSetAttribute(k_tile_sort<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem<false, 8192>()));
     }
+    if (tile == 4096) {
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<true, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<true, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<true, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<true, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 4096>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 4096>()));
+    } else {
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<true, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<true, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<true, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<true, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
+        KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
+    }
     g_attr_done[idx] = true;
     return 0;
 }
 
 // Kernel sequences shared by the plain and graph paths.
+static cudaError_t enq_tile_warp(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
+    if (L.prof) L.prof->kernel = prefix ? (keyed ? K_WARP_PREFIX_KEYED : K_WARP_PREFIX) : (keyed ? K_WARP_RANK_KEYED : K_WARP_RANK);
+    const int g = L.grid_warp;
+    if (L.tile_cap == 4096) {
+        if (prefix) {
+            const size_t sm = warp_smem<true, 4096>();
+            return keyed ? L.go(k_tile_warp<true, true, 4096>, g, TPB, sm, a) : L.go(k_tile_warp<true, false, 4096>, g, TPB, sm, a);
+        }
+        const size_t sm = warp_smem<false, 4096>();
+        return keyed ? L.go(k_tile_warp<false, true, 4096>, g, TPB, sm, a) : L.go(k_tile_warp<false, false, 4096>, g, TPB, sm, a);
+    }
+    if (prefix) {
+        const size_t sm = warp_smem<true, 8192>();
+        return keyed ? L.go(k_tile_warp<true, true, 8192>, g, TPB, sm, a) : L.go(k_tile_warp<true, false, 8192>, g, TPB, sm, a);
+    }
+    const size_t sm = warp_smem<false, 8192>();
+    return keyed ? L.go(k_tile_warp<false, true, 8192>, g, TPB, sm, a) : L.go(k_tile_warp<false, false, 8192>, g, TPB, sm, a);
+}
+
+static cudaError_t enq_tile_block(Launcher &L, const FwdArgs &a, bool prefix, bool keyed);
+
+// one small-group list: the block kernel for tiles holding a longer group, then the warp kernel for the others
 static cudaError_t enq_tile(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
+    const u32 el = L.prof ? L.prof->elems : 0, sg = L.prof ? L.prof->segs : 0;
+    cudaError_t e = enq_tile_block(L, a, prefix, keyed);
+    if (e || !a.warp_path) return e;
+    if (L.prof) L.prof->tag(0, el, sg);
+    return enq_tile_warp(L, a, prefix, keyed);
+}
+
+static cudaError_t enq_tile_block(Launcher &L, const FwdArgs &a, bool prefix, bool keyed) {
     if (L.prof) L.prof->kernel = prefix ? (keyed ? K_TILE_PREFIX_KEYED : K_TILE_PREFIX) : (keyed ? K_TILE_RANK_KEYED : K_TILE_RANK);
     if (L.tile_cap == 4096) {
         if (prefix) {
@@ -1099,7 +1446,7 @@ int FwdEngine::run_plain(cudaStream_t s) {
                           B, smax);
     set_caps(a);
     prof.reset();
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, &stats.launches, prof.on ? &prof : nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, &stats.launches, prof.on ? &prof : nullptr};
     auto cnt_e = [&](u32 l) { return (u32)h_ctl->cnt[l]; };
     auto cnt_s = [&](u32 l) { return (u32)(h_ctl->cnt[l] >> 32); };
     prof.round = 0; prof.pass = 0;
@@ -1140,10 +1487,25 @@ int FwdEngine::run_plain(cudaStream_t s) {
             more = cnt_e(lin) > 0;
         }
         prof.pass = -1;
-        if (prof.on) prof.tag(0, cnt_e(L_S0 + h_ctl->rpar), cnt_s(L_S0 + h_ctl->rpar));
-        KGB_CHECK(enq_tile(L, a, prefix, false));
-        if (prof.on) prof.tag(0, cnt_e(L_KS), cnt_s(L_KS));
-        KGB_CHECK(enq_tile(L, a, prefix, true));
+        if (prof.on) {
+            // one kernel at a time, with the control block read after each, so every record carries the elements
+            // that kernel itself sorted (tiles split between the block and the warp kernel)
+            for (int keyed = 0; keyed < 2; keyed++) {
+                const u32 lid = keyed ? L_KS : L_S0 + h_ctl->rpar;
+                const u32 segs = cnt_s(lid);
+                for (int wk = 0; wk < 2; wk++) {
+                    if (wk && !cfg.warp_path) break;
+                    const u64 before = h_ctl->tile_elems[wk];
+                    prof.tag(0, 0, segs);
+                    KGB_CHECK(wk ? enq_tile_warp(L, a, prefix, keyed) : enq_tile_block(L, a, prefix, keyed));
+                    if (int rc = read_ctl()) return rc;
+                    prof.recs.back().elems = (u32)(h_ctl->tile_elems[wk] - before);
+                }
+            }
+        } else {
+            KGB_CHECK(enq_tile(L, a, prefix, false));
+            KGB_CHECK(enq_tile(L, a, prefix, true));
+        }
         L.tag(K_CTL, 0);
         KGB_CHECK(L.go(k_ctl_round_end, 1, 1, 0, a));
         stats.rounds++;
@@ -1240,7 +1602,7 @@ int FwdEngine::build_graph(cudaStream_t s) {
                           B, smax);
     set_caps(a);
     long long dummy = 0;
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, &dummy, nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, &dummy, nullptr};
     Deps deps;
     if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
             return L.go(k_init, L.grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
@@ -1270,6 +1632,7 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     // persistent grids: as many CTAs as are resident at once (rank tiles: 3 per SM at 4096, prefix tiles: 2)
     grid_tile = sm_count * (cfg.tile_cap == 4096 ? std::min(std::max(cfg.tile_ctas, 1), 2) : 1);
     grid_tile_prefix = sm_count * (cfg.tile_cap == 4096 ? 2 : 1);
+    grid_warp = sm_count * (cfg.tile_cap == 4096 ? 4 : 2);
     grid_msd = sm_count * cfg.msd_ctas;
     grid_scan = sm_count * 4;
     // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan

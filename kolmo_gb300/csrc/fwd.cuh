@@ -35,6 +35,7 @@ struct ListView {
     u32 *ekey;  // element: current sort key (rank rounds), may be null
     Seg *seg;   // segment descriptors
     u32 *tmap;  // tile map (see fwd.cu)
+    u32 *tbig;  // small lists: per tile window, the round stamp of a group longer than WARP_GROUP starting there
 };
 
 // Device-resident control block of one forward sort (read by every kernel, written by the 1-thread control
@@ -49,13 +50,15 @@ struct Ctl {
     u32 err;
     u32 maxrounds;
     u32 pad;
+    u64 tile_elems[2];  // elements sorted so far by the block-level and the warp-level tile kernels (statistics)
 };
 
 struct FwdConfig {
     int tile_cap = 4096;  // small-group tile capacity: 4096 or 8192 (groups up to tile_cap / 2 go to the tiles)
     int tile_ctas = 2;    // persistent CTAs per SM for the tile sorter
-    int msd_ctas = 4;     // persistent CTAs per SM for the bucket passes
+    int msd_ctas = 8;     // persistent CTAs per SM for the bucket passes
     int small_group = 64; // tiles whose groups are all at most this long skip the radix passes (counting sort)
+    int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
 };
 
 struct FwdStats {
@@ -128,6 +131,7 @@ class FwdEngine {
     BlockInfo *d_blk = nullptr;
     ListView lists[NLISTS];
     u32 *d_hist = nullptr, *d_cursor = nullptr, *d_bhead = nullptr, *d_orand = nullptr;
+    u64 *d_orand64 = nullptr;
     u8 *d_dest = nullptr;
     Ctl *d_ctl = nullptr;
     Ctl *h_ctl = nullptr;  // pinned mirror
@@ -141,7 +145,7 @@ class FwdEngine {
     int graph_cap_key = 0;
     u64 graph_key = 0;
     int sm_count = 0;
-    int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0;
+    int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0, grid_warp = 0;
 };
 
 }  // namespace kgb

@@ -38,6 +38,8 @@ class Prof(ctypes.Structure):
 
 
 PLAIN = 1
+OPT_SMALL_GROUP = 1
+OPT_WARP_PATH = 2
 
 _lib = None
 
@@ -69,8 +71,8 @@ def lib():
     L.kgbwt_engine_destroy.argtypes = [_P]
     L.kgbwt_engine_config.argtypes = [_P, _I32, _I32, _I32]
     L.kgbwt_engine_config.restype = _I32
-    L.kgbwt_engine_small_group.argtypes = [_P, _I32]
-    L.kgbwt_engine_small_group.restype = _I32
+    L.kgbwt_engine_option.argtypes = [_P, _I32, _I32]
+    L.kgbwt_engine_option.restype = _I32
     L.kgbwt_engine_fwd.argtypes = [_P, _P, _P, _P, _P, ctypes.POINTER(Block), _I32, _P, _U32]
     L.kgbwt_engine_fwd.restype = _I32
     L.kgbwt_engine_inv.argtypes = [_P, _P, _P, ctypes.POINTER(IBlock), _I32, _P, _U32]
@@ -104,6 +106,6 @@ EXPORTS = (
     "kolmo_sais_bwt_aux", "kolmo_sais_unbwt_aux", "kolmo_sais_unbwt", "kgbwt_fwd_batch", "kgbwt_inv_batch",
     "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
     "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
-    "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_small_group",
+    "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_option",
     "kgbwt_unbwt_noalloc",
 )
