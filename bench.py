@@ -221,7 +221,7 @@ def run_ours(args, world, rank, local):
     ns = n_samples(n, r)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
-    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path)
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0)
     dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
     dT[:n] = torch.from_numpy(T).to(dev)
     dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
@@ -282,7 +282,8 @@ def run_ours(args, world, rank, local):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
                 "fwd_ms": round(sum(tf) / len(tf), 3), "inv_ms": round(sum(ti) / len(ti), 3),
                 "block_bytes": n, "skip_extras": True,
-                "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path]}
+                "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path,
+                        args.lsd_round0]}
 
     # profiled pass (plain path, CUDA events around every launch on stream s)
     eng.profile(True)
@@ -445,6 +446,7 @@ def main():
     ap.add_argument("--msd-ctas", type=int, default=0)
     ap.add_argument("--small-group", type=int, default=-1)
     ap.add_argument("--warp-path", type=int, default=-1)
+    ap.add_argument("--lsd-round0", type=int, default=-1)
     ap.add_argument("--profile-out", default="", help="write the per-launch profile of the profiled step here")
     ap.add_argument("--plain", action="store_true",
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")

@@ -88,9 +88,12 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
 /* Tuning options (results never depend on them). Returns 0 or -1 for an unknown option or value.
  * KGBWT_OPT_SMALL_GROUP (0..1024, default 64): tiles whose groups are all at most this long are sorted by counting
  *   inside each group instead of radix passes (0: always radix).
- * KGBWT_OPT_WARP_PATH (0/1, default 1): tiles whose groups are all at most 32 long go to the warp-level kernel. */
+ * KGBWT_OPT_WARP_PATH (0/1, default 1): tiles whose groups are all at most 32 long go to the warp-level kernel.
+ * KGBWT_OPT_LSD_ROUND0 (0/1, default 1): the first round (all suffixes by their 8-byte prefix) is one LSD radix
+ *   sort of the whole batch; 0: bucket passes and tile kernels as in the later rounds. */
 #define KGBWT_OPT_SMALL_GROUP 1
 #define KGBWT_OPT_WARP_PATH 2
+#define KGBWT_OPT_LSD_ROUND0 3
 int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value);
 /* Forward: text blocks in dT (16 readable bytes past the last block). Results: dL receives each block's L column
  * with its sentinel row (n + 1 bytes at off + block index; row p0 holds no text byte), dI the sampled indexes at

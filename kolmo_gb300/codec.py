@@ -104,15 +104,16 @@ class Engine:
             self.config(tile_cap, tile_ctas, msd_ctas)
 
     def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1,
-               warp_path: int = -1):
+               warp_path: int = -1, lsd_round0: int = -1):
         L = native.lib()
         rc = L.kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
-        if rc == 0 and small_group >= 0:
-            rc = L.kgbwt_engine_option(self.h, native.OPT_SMALL_GROUP, small_group)
-        if rc == 0 and warp_path >= 0:
-            rc = L.kgbwt_engine_option(self.h, native.OPT_WARP_PATH, warp_path)
+        for opt, val in ((native.OPT_SMALL_GROUP, small_group), (native.OPT_WARP_PATH, warp_path),
+                         (native.OPT_LSD_ROUND0, lsd_round0)):
+            if rc == 0 and val >= 0:
+                rc = L.kgbwt_engine_option(self.h, opt, val)
         if rc:
-            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group} {warp_path}")
+            raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group} {warp_path} "
+                             f"{lsd_round0}")
 
     def close(self):
         if self.h:

@@ -20,6 +20,7 @@ const char *kernel_name(int k) {
         "init", "fixup", "keygen", "msd_hist", "msd_scan", "msd_scatter", "tile_sort_prefix", "tile_sort_prefix_keyed",
         "tile_sort_rank", "tile_sort_rank_keyed", "control", "samples",
         "tile_warp_prefix", "tile_warp_prefix_keyed", "tile_warp_rank", "tile_warp_rank_keyed",
+        "lsd_begin", "lsd_key0", "lsd_hist", "lsd_pass", "seg_count", "seg_scan", "seg_emit1", "seg_emit2",
         "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
@@ -276,6 +277,10 @@ int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
         case KGBWT_OPT_WARP_PATH:
             if (value != 0 && value != 1) return -1;
             e->fwd.cfg.warp_path = value;
+            return 0;
+        case KGBWT_OPT_LSD_ROUND0:
+            if (value != 0 && value != 1) return -1;
+            e->fwd.cfg.lsd_round0 = value;
             return 0;
         default:
             return -1;

@@ -29,6 +29,7 @@
 #include <type_traits>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 
 namespace kgb {
 
@@ -61,6 +62,12 @@ struct FwdArgs {
     u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
     u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
+    // round 0 as an LSD radix sort
+    u64 *lkey[2];
+    u32 *lval[2], *lhi[2];
+    u64 *lstat;
+    u32 *lhist, *ltile, *segagg;
+    u32 spin_limit;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segl, cap_tms, cap_tml;
 };
@@ -1083,6 +1090,8 @@ __global__ void k_init(FwdArgs a, const u32 *__restrict__ blk_list_start, const 
     }
 }
 
+#include "fwd_lsd.cuh"
+
 // ------------------------------------------------------------------------------------------------ host engine
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -1150,6 +1159,16 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     add((void **)&d_dest, nseg_large * 256);
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
+    const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
+    for (int q = 0; q < 2; q++) {
+        add((void **)&d_lkey[q], n * 8);
+        add((void **)&d_lval[q], n * 4);
+        add((void **)&d_lhi[q], n * 4);
+    }
+    add((void **)&d_lstat, ltiles * 256 * 8);
+    add((void **)&d_lhist, NSLOT * 256 * 4);
+    add((void **)&d_ltile, 64);
+    add((void **)&d_segagg, stiles * 8 * 4);
     add((void **)&d_ctl, sizeof(Ctl));
     size_t total = 0;
     for (auto &it : items) total += it.bytes;
@@ -1180,11 +1199,16 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     Icap = icap;
     sa_cap = want_sa;
     cap_segs = nseg_small; cap_segl = nseg_large; cap_tms = ntm_small; cap_tml = ntm_large;
+    lsd_tiles_cap = ltiles; seg_tiles_cap = stiles;
+    KGB_CHECK(cudaMemset(d_lstat, 0, ltiles * 256 * 8));
     return 0;
 }
 
 void FwdEngine::set_caps(FwdArgs &a) const {
     a.orand64 = d_orand64;
+    for (int q = 0; q < 2; q++) { a.lkey[q] = d_lkey[q]; a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
+    a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg;
+    a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.warp_path = (u32)cfg.warp_path;
     a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_tms = cap_tms; a.cap_tml = cap_tml;
@@ -1236,17 +1260,21 @@ int FwdEngine::plan_external(const u32 *off, const u32 *n, const u32 *r, const u
 
 static int ceil_log2(u64 x) { int k = 0; while ((1ull << k) < x) k++; return k; }
 
+bool FwdEngine::lsd_enabled() const { return cfg.lsd_round0 && N < (1ull << 30); }
+
 int FwdEngine::setup_round0(cudaStream_t s) {
     // block table, round-0 lists and their tile maps are laid out on the host (B entries, small)
     const u32 smax = (u32)cfg.tile_cap / 2;
     std::vector<BlockInfo> bi(B);
+    u32 soff_b = 0;
     std::vector<u32> lstart(B);
     std::vector<u8> large(B);
     std::vector<Seg> seg_s, seg_l;
     std::vector<u32> tm_s, tm_l, big_s;
     u64 es = 0, el = 0;
     for (u32 b = 0; b < B; b++) {
-        bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b]};
+        bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b], soff_b, 0};
+        soff_b += h_n[b];
         large[b] = h_n[b] > smax;
         Seg g;
         g.len = h_n[b]; g.head = 0; g.bd = b;
@@ -1270,6 +1298,7 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     c.cnt[L_S0] = ((u64)seg_s.size() << 32) | es;
     c.cnt[L_L0] = ((u64)seg_l.size() << 32) | el;
     c.maxrounds = (u32)ceil_log2(maxn) + 3;
+    c.seq = ++call_seq;
     KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
     const size_t ntm = cap_tms;
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemsetAsync(lists[l].tbig, 0xFF, ntm * 4, s));
@@ -1312,6 +1341,7 @@ static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const
     return a;
 }
 
+static size_t lsd_smem() { return sizeof(LsdSmem); }
 template <bool PREFIX, int TILE>
 static int tile_smem() { return (int)sizeof(TileSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
 template <bool PREFIX, int TILE>
@@ -1319,7 +1349,7 @@ static int warp_smem() { return (int)sizeof(WarpSmem<TILE, typename TileTraits<P
 
 struct Launcher {
     cudaStream_t s;
-    int grid_tile, grid_msd, grid_scan, tile_cap, grid_tile_prefix, grid_warp;
+    int grid_tile, grid_msd, grid_scan, tile_cap, grid_tile_prefix, grid_warp, grid_lsd;
     long long *launches;
     Profiler *prof;
     template <typename K, typename... Args>
@@ -1360,6 +1390,7 @@ static int set_tile_attrs(int tile) {
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
     }
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
     g_attr_done[idx] = true;
     return 0;
 }
@@ -1440,71 +1471,123 @@ static int report_err(u32 bits) {
     return -2;
 }
 
+
+// Round 0 as an LSD radix sort, in two parts: begin, keys and the first histogram; then the radix passes (one per
+// slot in `slots`; each returns at once when its key byte does not vary) and the segmentation.
+static cudaError_t enq_lsd_keys(Launcher &L, const FwdArgs &a) {
+    cudaError_t e;
+    L.tag(K_LSD_BEGIN, 0);
+    if ((e = L.go(k_lsd_begin, 1, 256, 0, a))) return e;
+    L.tag(K_LSD_KEY0, 0);
+    if ((e = L.go(k_lsd_key0, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_LSD_HIST, 0);
+    return L.go(k_lsd_hist0, L.grid_msd, TPB, 0, a);
+}
+static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u32 m_tag) {
+    cudaError_t e;
+    for (int slot = 0; slot < NSLOT; slot++) {
+        if (!((slots >> slot) & 1)) continue;
+        L.tag(K_LSD_PASS, m_tag);
+        if (L.prof) L.prof->pass = slot;
+        if ((e = L.go(k_lsd_pass, L.grid_lsd, TPB, lsd_smem(), a, slot))) return e;
+    }
+    if (L.prof) L.prof->pass = -1;
+    L.tag(K_SEG_COUNT, m_tag);
+    if ((e = L.go(k_seg_count, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_SEG_SCAN, m_tag);
+    if ((e = L.go(k_seg_scan, 1, 1024, 0, a))) return e;
+    L.tag(K_SEG_EMIT1, m_tag);
+    if ((e = L.go(k_seg_emit1, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_SEG_EMIT2, m_tag);
+    return L.go(k_seg_emit2, L.grid_msd, TPB, 0, a);
+}
+
+static u32 host_active_slots(const Ctl &c) {
+    const u64 vl = c.vary_lo ^ c.and_lo;
+    const u32 vh = c.vary_hi ^ c.and_hi;
+    u32 m = 0;
+    for (int q = 0; q < 8; q++) if ((vl >> (8 * q)) & 0xFF) m |= 1u << q;
+    for (int q = 0; q < 4; q++) if ((vh >> (8 * q)) & 0xFF) m |= 1u << (8 + q);
+    return m;
+}
+
 int FwdEngine::run_plain(cudaStream_t s) {
     const u32 smax = (u32)cfg.tile_cap / 2;
     FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
                           B, smax);
     set_caps(a);
     prof.reset();
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, &stats.launches, prof.on ? &prof : nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, grid_lsd, &stats.launches, prof.on ? &prof : nullptr};
     auto cnt_e = [&](u32 l) { return (u32)h_ctl->cnt[l]; };
     auto cnt_s = [&](u32 l) { return (u32)(h_ctl->cnt[l] >> 32); };
-    prof.round = 0; prof.pass = 0;
-    L.tag(K_INIT, (u32)N, B);
-    KGB_CHECK(L.go(k_init, grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
     auto read_ctl = [&]() -> int {
         KGB_CHECK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
         KGB_CHECK(cudaStreamSynchronize(s));
         return 0;
     };
+    prof.round = 0; prof.pass = 0;
+    const bool lsd0 = lsd_enabled();
+    if (!lsd0) {
+        L.tag(K_INIT, (u32)N, B);
+        KGB_CHECK(L.go(k_init, grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest));
+    }
     if (int rc = read_ctl()) return rc;
     for (int round = 0;; round++) {
         const bool prefix = round == 0;
         const u32 rp = h_ctl->rpar;
         prof.round = round; prof.pass = -1;
-        if (!prefix) {
-            L.tag(K_FIXUP, cnt_e(L_R0 + (rp ^ 1)));
-            KGB_CHECK(L.go(k_fixup, grid_msd, TPB, 0, a));
-            L.tag(K_KEYGEN, cnt_e(L_L0 + rp), cnt_s(L_L0 + rp));
-            KGB_CHECK(L.go(k_keygen, grid_msd, TPB, 0, a));
-        }
-        L.tag(K_CTL, 0);
-        KGB_CHECK(L.go(k_ctl_msd_begin, 1, 1, 0, a));
-        if (int rc = read_ctl()) return rc;
-        u32 lin = L_L0 + h_ctl->rpar;
-        u32 more = cnt_e(lin) > 0;
-        int pass = 0;
-        while (more) {
-            prof.pass = pass++;
-            L.tag(K_MSD_HIST, cnt_e(lin), cnt_s(lin));
-            KGB_CHECK(enq_msd_pass(L, a, prefix));
-            L.tag(K_CTL, 0);
-            KGB_CHECK(L.go(k_ctl_msd_next, 1, 1, 0, a));
-            stats.passes++;
+        if (prefix && lsd0) {
+            // LSD round 0: launch only the passes whose key byte varies (the host reads them after the keys)
+            KGB_CHECK(enq_lsd_keys(L, a));
             if (int rc = read_ctl()) return rc;
-            if (h_ctl->err) return report_err(h_ctl->err);
-            lin = L_K0 + ((h_ctl->pass - 1) & 1);
-            more = cnt_e(lin) > 0;
-        }
-        prof.pass = -1;
-        if (prof.on) {
-            // one kernel at a time, with the control block read after each, so every record carries the elements
-            // that kernel itself sorted (tiles split between the block and the warp kernel)
-            for (int keyed = 0; keyed < 2; keyed++) {
-                const u32 lid = keyed ? L_KS : L_S0 + h_ctl->rpar;
-                const u32 segs = cnt_s(lid);
-                for (int wk = 0; wk < 2; wk++) {
-                    if (wk && !cfg.warp_path) break;
-                    const u64 before = h_ctl->tile_elems[wk];
-                    prof.tag(0, 0, segs);
-                    KGB_CHECK(wk ? enq_tile_warp(L, a, prefix, keyed) : enq_tile_block(L, a, prefix, keyed));
-                    if (int rc = read_ctl()) return rc;
-                    prof.recs.back().elems = (u32)(h_ctl->tile_elems[wk] - before);
-                }
-            }
+            const u32 slots = host_active_slots(*h_ctl);
+            KGB_CHECK(enq_lsd_sort_seg(L, a, slots, (u32)N));
+            stats.passes += __builtin_popcount(slots);
         } else {
-            KGB_CHECK(enq_tile(L, a, prefix, false));
-            KGB_CHECK(enq_tile(L, a, prefix, true));
+            if (!prefix) {
+                L.tag(K_FIXUP, cnt_e(L_R0 + (rp ^ 1)));
+                KGB_CHECK(L.go(k_fixup, grid_msd, TPB, 0, a));
+                L.tag(K_KEYGEN, cnt_e(L_L0 + rp), cnt_s(L_L0 + rp));
+                KGB_CHECK(L.go(k_keygen, grid_msd, TPB, 0, a));
+            }
+            L.tag(K_CTL, 0);
+            KGB_CHECK(L.go(k_ctl_msd_begin, 1, 1, 0, a));
+            if (int rc = read_ctl()) return rc;
+            u32 lin = L_L0 + h_ctl->rpar;
+            u32 more = cnt_e(lin) > 0;
+            int pass = 0;
+            while (more) {
+                prof.pass = pass++;
+                L.tag(K_MSD_HIST, cnt_e(lin), cnt_s(lin));
+                KGB_CHECK(enq_msd_pass(L, a, prefix));
+                L.tag(K_CTL, 0);
+                KGB_CHECK(L.go(k_ctl_msd_next, 1, 1, 0, a));
+                stats.passes++;
+                if (int rc = read_ctl()) return rc;
+                if (h_ctl->err) return report_err(h_ctl->err);
+                lin = L_K0 + ((h_ctl->pass - 1) & 1);
+                more = cnt_e(lin) > 0;
+            }
+            prof.pass = -1;
+            if (prof.on) {
+                // one kernel at a time, with the control block read after each, so every record carries the elements
+                // that kernel itself sorted (tiles split between the block and the warp kernel)
+                for (int keyed = 0; keyed < 2; keyed++) {
+                    const u32 lid = keyed ? L_KS : L_S0 + h_ctl->rpar;
+                    const u32 segs = cnt_s(lid);
+                    for (int wk = 0; wk < 2; wk++) {
+                        if (wk && !cfg.warp_path) break;
+                        const u64 before = h_ctl->tile_elems[wk];
+                        prof.tag(0, 0, segs);
+                        KGB_CHECK(wk ? enq_tile_warp(L, a, prefix, keyed) : enq_tile_block(L, a, prefix, keyed));
+                        if (int rc = read_ctl()) return rc;
+                        prof.recs.back().elems = (u32)(h_ctl->tile_elems[wk] - before);
+                    }
+                }
+            } else {
+                KGB_CHECK(enq_tile(L, a, prefix, false));
+                KGB_CHECK(enq_tile(L, a, prefix, true));
+            }
         }
         L.tag(K_CTL, 0);
         KGB_CHECK(L.go(k_ctl_round_end, 1, 1, 0, a));
@@ -1557,12 +1640,24 @@ static int add_while(cudaGraph_t g, Deps &deps, cudaGraphConditionalHandle h, cu
     return 0;
 }
 
-// One round (prefix or rank) into graph g after deps; hmsd closes its bucket-pass loop, hround is set by its end.
-static int add_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L, const FwdArgs &a, bool prefix,
-                     cudaGraphConditionalHandle hmsd, cudaGraphConditionalHandle hround) {
-    FwdArgs am = a, ar = a;
+static int add_if(cudaGraph_t g, Deps &deps, cudaGraphConditionalHandle h, cudaGraph_t *body) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    KGB_CHECK(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &cp));
+    *body = cp.conditional.phGraph_out[0];
+    deps.assign(1, node);
+    return 0;
+}
+
+// A tile-path round (prefix or rank) into graph g after deps; hmsd closes its bucket-pass loop.
+static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L, const FwdArgs &a, bool prefix,
+                          cudaGraphConditionalHandle hmsd) {
+    FwdArgs am = a;
     am.hcond = (unsigned long long)hmsd;
-    ar.hcond = (unsigned long long)hround;
     if (int rc = capture_into(s, g, deps, [&]() -> cudaError_t {
             cudaError_t e;
             if (!prefix) {
@@ -1584,35 +1679,54 @@ static int add_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L, con
     return capture_into(s, g, deps, [&]() -> cudaError_t {
         cudaError_t e;
         if ((e = enq_tile(L, a, prefix, false))) return e;
-        if ((e = enq_tile(L, a, prefix, true))) return e;
-        return L.go(k_ctl_round_end, 1, 1, 0, ar);
+        return enq_tile(L, a, prefix, true);
     });
 }
 
+// Graph: round 0 (the LSD sort and segmentation, or the tile path's init + prefix round), round end, then
+// while (active) { rank round ; round end }, then the sampled indexes. The 1-thread round-end kernel sets the loop
+// handle; the bucket-pass loops have their own handles.
 int FwdEngine::build_graph(cudaStream_t s) {
     const u32 smax = (u32)cfg.tile_cap / 2;
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
     KGB_CHECK(cudaGraphCreate(&graph, 0));
-    cudaGraphConditionalHandle hround, hmsd0, hmsd;
+    // every handle created here belongs to exactly one conditional node below
+    const bool lsd = lsd_enabled();
+    cudaGraphConditionalHandle hround = 0, hmsd0 = 0, hmsd = 0;
     KGB_CHECK(cudaGraphConditionalHandleCreate(&hround, graph, 0, cudaGraphCondAssignDefault));
-    KGB_CHECK(cudaGraphConditionalHandleCreate(&hmsd0, graph, 0, cudaGraphCondAssignDefault));
+    if (!lsd) KGB_CHECK(cudaGraphConditionalHandleCreate(&hmsd0, graph, 0, cudaGraphCondAssignDefault));
     KGB_CHECK(cudaGraphConditionalHandleCreate(&hmsd, graph, 0, cudaGraphCondAssignDefault));
     FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
                           B, smax);
     set_caps(a);
+    FwdArgs ar = a;
+    ar.hcond = (unsigned long long)hround;
     long long dummy = 0;
-    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, &dummy, nullptr};
+    Launcher L{s, grid_tile, grid_msd, grid_scan, cfg.tile_cap, grid_tile_prefix, grid_warp, grid_lsd, &dummy, nullptr};
     Deps deps;
-    if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
-            return L.go(k_init, L.grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
-        }))
+    if (lsd) {
+        if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
+                cudaError_t e = enq_lsd_keys(L, a);
+                if (e) return e;
+                return enq_lsd_sort_seg(L, a, 0xFFFFFFFFu, 0);
+            }))
+            return rc;
+    } else {
+        if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
+                return L.go(k_init, L.grid_msd, TPB, 0, a, (const u32 *)d_cursor, (const u8 *)d_dest);
+            }))
+            return rc;
+        if (int rc = add_tile_round(s, graph, deps, L, a, true, hmsd0)) return rc;
+    }
+    if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t { return L.go(k_ctl_round_end, 1, 1, 0, ar); }))
         return rc;
-    if (int rc = add_round(s, graph, deps, L, a, true, hmsd0, hround)) return rc;
     cudaGraph_t rbody;
     if (int rc = add_while(graph, deps, hround, &rbody)) return rc;
     Deps rd;
-    if (int rc = add_round(s, rbody, rd, L, a, false, hmsd, hround)) return rc;
+    if (int rc = add_tile_round(s, rbody, rd, L, a, false, hmsd)) return rc;
+    if (int rc = capture_into(s, rbody, rd, [&]() -> cudaError_t { return L.go(k_ctl_round_end, 1, 1, 0, ar); }))
+        return rc;
     if (int rc = capture_into(s, graph, deps, [&]() -> cudaError_t {
             return L.go(k_samples, (int)std::min<u32>(B, 1024u), 128, 0, a);
         }))
@@ -1633,13 +1747,15 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     grid_tile = sm_count * (cfg.tile_cap == 4096 ? std::min(std::max(cfg.tile_ctas, 1), 2) : 1);
     grid_tile_prefix = sm_count * (cfg.tile_cap == 4096 ? 2 : 1);
     grid_warp = sm_count * (cfg.tile_cap == 4096 ? 4 : 2);
+    grid_lsd = (int)((N + LSD_TILE - 1) / LSD_TILE);
     grid_msd = sm_count * cfg.msd_ctas;
     grid_scan = sm_count * 4;
     // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan
     if (int rc = setup_round0(s)) return rc;
     if (!use_graph) return run_plain(s);
     const u64 key = ((u64)B << 40) ^ ((u64)N << 2) ^ ((u64)(uintptr_t)d_T) ^ ((u64)(uintptr_t)d_L << 1) ^
-                    ((u64)(uintptr_t)d_I << 3) ^ ((u64)(uintptr_t)d_SA << 5) ^ (u64)cfg.tile_cap ^ ((u64)Ncap << 7);
+                    ((u64)(uintptr_t)d_I << 3) ^ ((u64)(uintptr_t)d_SA << 5) ^ (u64)cfg.tile_cap ^ ((u64)Ncap << 7) ^
+                    ((u64)lsd_enabled() << 63);
     if (!gexec || key != graph_key) {
         // capture on the engine's own stream: the caller's may be the legacy default stream, which cannot capture
         if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));

@@ -12,6 +12,8 @@ struct FwdArgs;
 // bytes, sentinel row included) starts at off + index of the block; its sampled indexes start at `iout`.
 struct BlockInfo {
     u32 off, n, r, iout;
+    u32 soff;  // first position of the block in the dense order of all suffixes of the batch (prefix sum of n)
+    u32 pad;
 };
 
 // A segment of an element list: `len` consecutive elements starting at `start` that form one group (equal sort
@@ -51,6 +53,12 @@ struct Ctl {
     u32 maxrounds;
     u32 pad;
     u64 tile_elems[2];  // elements sorted so far by the block-level and the warp-level tile kernels (statistics)
+    // round 0 as an LSD radix sort
+    u64 vary_lo;        // OR / AND of the sort keys (which key bytes vary)
+    u64 and_lo;
+    u32 vary_hi, and_hi;
+    u32 m;              // suffixes sorted
+    u32 seq;            // call sequence number (tags the look-back words of the radix passes)
 };
 
 struct FwdConfig {
@@ -59,6 +67,7 @@ struct FwdConfig {
     int msd_ctas = 8;     // persistent CTAs per SM for the bucket passes
     int small_group = 64; // tiles whose groups are all at most this long skip the radix passes (counting sort)
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
+    int lsd_round0 = 1;   // round 0 (8-byte prefixes) as one LSD radix sort of all suffixes; 0: bucket passes + tiles
 };
 
 struct FwdStats {
@@ -108,6 +117,8 @@ class FwdEngine {
     void free_all();
     int setup_round0(cudaStream_t s);
     void set_caps(FwdArgs &a) const;
+    bool lsd_enabled() const;
+    u32 call_seq = 0;
     u64 cap_segs = 0, cap_segl = 0, cap_tms = 0, cap_tml = 0;
 
     // capacities
@@ -132,6 +143,12 @@ class FwdEngine {
     ListView lists[NLISTS];
     u32 *d_hist = nullptr, *d_cursor = nullptr, *d_bhead = nullptr, *d_orand = nullptr;
     u64 *d_orand64 = nullptr;
+    // LSD path
+    u64 *d_lkey[2] = {nullptr, nullptr};
+    u32 *d_lval[2] = {nullptr, nullptr}, *d_lhi[2] = {nullptr, nullptr};
+    u64 *d_lstat = nullptr;
+    u32 *d_lhist = nullptr, *d_ltile = nullptr, *d_segagg = nullptr;
+    u64 lsd_tiles_cap = 0, seg_tiles_cap = 0;
     u8 *d_dest = nullptr;
     Ctl *d_ctl = nullptr;
     Ctl *h_ctl = nullptr;  // pinned mirror
@@ -145,7 +162,7 @@ class FwdEngine {
     int graph_cap_key = 0;
     u64 graph_key = 0;
     int sm_count = 0;
-    int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0, grid_warp = 0;
+    int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0, grid_warp = 0, grid_lsd = 0;
 };
 
 }  // namespace kgb

@@ -1,0 +1,516 @@
+// Round 0 of the forward sort as one LSD radix sort: every suffix of the batch is sorted by (block, zero-padded
+// 8-byte prefix) with one pass per varying key byte (single-pass scatter with decoupled look-back), then a
+// segmentation turns the sorted keys into ranks, finished suffixes and the rank rounds' groups (the small-group list
+// for the tile kernels, the large-group list for the bucket passes). Included by fwd.cu inside namespace kgb, after
+// the kernels it shares (FwdArgs, resolve, tile-map writers).
+#pragma once
+// (included inside namespace kgb)
+
+constexpr int LSD_IPT = 12, LSD_TILE = TPB * LSD_IPT;  // elements per sort tile
+constexpr int NSLOT = 12;                              // digit slots: key bytes 0..7, then block-index bytes 0..3
+constexpr int SEG_IPT = 16, SEG_TILE = TPB * SEG_IPT;  // positions per segmentation tile (SEG_IPT <= 32)
+// look-back words: epoch (32 bits: call sequence, digit slot) | flag (2 bits) | value (30 bits); a word of another
+// epoch (an earlier slot or call) counts as not yet published
+constexpr u64 ST_AGG = 1ull << 30, ST_PRE = 2ull << 30, ST_VAL = (1ull << 30) - 1;
+constexpr u64 ST_EPOCH = 0xFFFFFFFF00000000ull;
+
+__device__ __forceinline__ u32 slot_digit(u64 k, u32 hi, int slot) {
+    return slot < 8 ? (u32)(k >> (8 * slot)) & 0xFFu : (hi >> (8 * (slot - 8))) & 0xFFu;
+}
+__device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte s varies in this round
+    const u64 vl = c->vary_lo ^ c->and_lo;
+    const u32 vh = c->vary_hi ^ c->and_hi;
+    u32 m = 0;
+#pragma unroll
+    for (int s = 0; s < 8; s++) m |= ((vl >> (8 * s)) & 0xFF) ? 1u << s : 0u;
+#pragma unroll
+    for (int s = 0; s < 4; s++) m |= ((vh >> (8 * s)) & 0xFF) ? 1u << (8 + s) : 0u;
+    return m;
+}
+__device__ __forceinline__ bool lsd_has_hi(const FwdArgs &a) { return a.ctl->round == 0 && a.B > 1; }
+
+// Round start (256 threads): clear the digit histograms, the key OR/AND and the tile counters.
+__global__ void k_lsd_begin(FwdArgs a) {
+    Ctl *c = a.ctl;
+    for (int i = threadIdx.x; i < NSLOT * 256; i += blockDim.x) a.lhist[i] = 0;
+    if (threadIdx.x < NSLOT) a.ltile[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        c->vary_lo = 0; c->and_lo = ~0ull; c->vary_hi = 0; c->and_hi = ~0u;
+        c->cnt[L_R0 + c->rpar] = 0;
+    }
+}
+
+__device__ __forceinline__ void orand_flush(Ctl *c, u64 ol, u64 al, u32 oh, u32 ah) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        ol |= __shfl_xor_sync(0xffffffffu, ol, o);
+        al &= __shfl_xor_sync(0xffffffffu, al, o);
+        oh |= __shfl_xor_sync(0xffffffffu, oh, o);
+        ah &= __shfl_xor_sync(0xffffffffu, ah, o);
+    }
+    if (lane_id() == 0) {
+        if (ol) atomicOr(&c->vary_lo, ol);
+        if (al != ~0ull) atomicAnd(&c->and_lo, al);
+        if (oh) atomicOr(&c->vary_hi, oh);
+        if (ah != ~0u) atomicAnd(&c->and_hi, ah);
+    }
+}
+
+// Round 0 keys: the zero-padded 8-byte prefix of every suffix (block index in `hi` when the batch has several
+// blocks), in the dense order of the batch.
+__global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
+    Ctl *c = a.ctl;
+    const bool hi = a.B > 1;
+    const u64 stride = (u64)gridDim.x * blockDim.x;
+    u64 ol = 0, al = ~0ull;
+    u32 oh = 0, ah = ~0u;
+    for (u32 b = 0; b < a.B; b++) {
+        const BlockInfo bi = a.blk[b];
+        const u64 end = (u64)bi.off + bi.n;
+        // row 0 of the L column (the sentinel rotation) holds the block's last byte
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
+        for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < bi.n; j += stride) {
+            const u32 id = bi.off + (u32)j;
+            u64 k = load_be64(a.T, id);
+            const u64 rem = end - id;
+            if (rem < 8) k &= ~0ull << (8 * (8 - rem));
+            const u64 x = (u64)bi.soff + j;
+            a.lkey[0][x] = k;
+            a.lval[0][x] = id;
+            if (hi) a.lhi[0][x] = b;
+            ol |= k; al &= k; oh |= b; ah &= b;
+        }
+    }
+    if (!hi) { oh = 0; ah = 0; }
+    orand_flush(c, ol, al, oh, ah);
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->m = a.B ? a.blk[a.B - 1].soff + a.blk[a.B - 1].n : 0;
+}
+
+// Histogram of the lowest varying digit (the first pass); later passes build their successor's histogram.
+__global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
+    __shared__ u32 hs[256];
+    const Ctl *c = a.ctl;
+    const u32 act = active_slots(c);
+    if (!act) return;
+    const int slot = __ffs(act) - 1;
+    const bool hi = lsd_has_hi(a);
+    const u32 m = c->m;
+    hs[threadIdx.x] = 0;
+    __syncthreads();
+    const u32 lane = lane_id();
+    for (u32 x0 = blockIdx.x * blockDim.x; x0 < m; x0 += gridDim.x * blockDim.x) {
+        const u32 x = x0 + threadIdx.x;
+        u32 d = 0x100;
+        if (x < m) d = slot_digit(a.lkey[0][x], hi ? a.lhi[0][x] : 0u, slot);
+        const u32 peers = __match_any_sync(0xffffffffu, d);
+        if (d < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&hs[d], __popc(peers));
+    }
+    __syncthreads();
+    if (hs[threadIdx.x]) atomicAdd(&a.lhist[slot * 256 + threadIdx.x], hs[threadIdx.x]);
+}
+
+struct LsdSmem {
+    u64 key[LSD_TILE];
+    u32 val[LSD_TILE];
+    u32 hi[LSD_TILE];
+    u16 wcnt[TPB / 32][256];
+    u32 dstart[256];
+    u64 gbase[256];
+    u32 dbase[256];
+    u32 nh[256];
+    u32 ws[TPB / 32 + 1];
+    u32 tile;
+};
+
+// One LSD pass over digit `slot` (skipped when that key byte is the same in every key): rank the tile's keys by
+// digit, publish the tile's digit counts, look back over earlier tiles for the global offsets (bounded spin), stage
+// the tile in shared memory in digit order and write it out in runs; meanwhile count the next varying digit.
+__global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
+    const Ctl *c = a.ctl;
+    const u32 act = active_slots(c);
+    if (!((act >> slot) & 1)) return;
+    const u32 par = __popc(act & ((1u << slot) - 1)) & 1;
+    const u32 nxt_mask = act & ~((2u << slot) - 1);
+    const int nslot = nxt_mask ? __ffs(nxt_mask) - 1 : -1;
+    const bool hi = lsd_has_hi(a);
+    const u32 m = c->m;
+    const u32 ntiles = (m + LSD_TILE - 1) / LSD_TILE;
+    const u64 epoch = (u64)((c->seq << 4) | (u32)slot) << 32;
+    const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
+    if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
+    // digit bases of the pass: exclusive scan of the slot's histogram
+    {
+        const u32 hcount = a.lhist[slot * 256 + tid];
+        S.dbase[tid] = block_excl_sum<TPB>(hcount, S.ws, nullptr);
+    }
+    for (int i = tid; i < (TPB / 32) * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
+    S.nh[tid] = 0;
+    __syncthreads();
+    const u32 tile = S.tile;
+    if (tile >= ntiles) return;
+    const u32 base = tile * LSD_TILE;
+    const u32 cnt = min((u32)LSD_TILE, m - base);
+    const u64 *kin = a.lkey[par];
+    const u32 *vin = a.lval[par], *hin = a.lhi[par];
+    u64 k[LSD_IPT];
+    u32 v[LSD_IPT], hh[LSD_IPT], dg[LSD_IPT], rk[LSD_IPT];
+#pragma unroll
+    for (int j = 0; j < LSD_IPT; j++) {
+        const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
+        const bool ok = x < cnt;
+        k[j] = ok ? kin[base + x] : 0ull;
+        v[j] = ok ? vin[base + x] : 0u;
+        hh[j] = ok && hi ? hin[base + x] : 0u;
+        dg[j] = ok ? slot_digit(k[j], hh[j], slot) : 0x100u;
+    }
+#pragma unroll
+    for (int j = 0; j < LSD_IPT; j++) {
+        const u32 d = dg[j];
+        const u32 peers = __match_any_sync(0xffffffffu, d);
+        const u32 before = d < 256 ? S.wcnt[warp][d] : 0u;
+        rk[j] = before + __popc(peers & lanemask_lt());
+        __syncwarp();
+        if (d < 256 && (__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
+        __syncwarp();
+    }
+    __syncthreads();
+    // thread tid owns digit tid: tile count, publish, local start, look back
+    u32 tot = 0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; w++) tot += S.wcnt[w][tid];
+    u64 *st = a.lstat + (u64)tile * 256 + tid;
+    if (tile == 0) atomicExch((unsigned long long *)st, epoch | ST_PRE | tot);
+    else atomicExch((unsigned long long *)st, epoch | ST_AGG | tot);
+    u32 dstart = block_excl_sum<TPB>(tot, S.ws, nullptr);
+    S.dstart[tid] = dstart;
+    {
+        u32 run = dstart;
+#pragma unroll
+        for (int w = 0; w < TPB / 32; w++) { const u32 cc = S.wcnt[w][tid]; S.wcnt[w][tid] = (u16)run; run += cc; }
+    }
+    u64 excl = 0;
+    if (tile > 0) {
+        long j = (long)tile - 1;
+        u32 spins = 0;
+        while (j >= 0) {
+            const u64 w = *(volatile u64 *)(a.lstat + (u64)j * 256 + tid);
+            if ((w & ST_EPOCH) != epoch || !(w & (ST_AGG | ST_PRE))) {
+                if (++spins > a.spin_limit) {  // a predecessor never published: report and stop waiting
+                    atomicOr(&a.ctl->err, 256u);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += w & ST_VAL;
+            if (w & ST_PRE) break;
+            j--;
+        }
+        atomicExch((unsigned long long *)st, epoch | ST_PRE | (excl + tot));
+    }
+    S.gbase[tid] = (u64)S.dbase[tid] + excl - dstart;
+    __syncthreads();
+    // stage in digit order
+#pragma unroll
+    for (int j = 0; j < LSD_IPT; j++) {
+        if (dg[j] < 256) {
+            const u32 p = S.wcnt[warp][dg[j]] + rk[j];
+            S.key[p] = k[j];
+            S.val[p] = v[j];
+            S.hi[p] = hh[j];
+        }
+    }
+    __syncthreads();
+    u64 *kout = a.lkey[par ^ 1];
+    u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1];
+    for (u32 i = tid; i < LSD_TILE; i += TPB) {
+        u32 d2 = 0x100;
+        if (i < cnt) {
+            const u64 kk = S.key[i];
+            const u32 h2 = S.hi[i];
+            const u64 dst = S.gbase[slot_digit(kk, h2, slot)] + i;
+            if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
+                kout[dst] = kk;
+                vout[dst] = S.val[i];
+                if (hi) hout[dst] = h2;
+            }
+            if (nslot >= 0) d2 = slot_digit(kk, h2, nslot);
+        }
+        if (nslot >= 0) {
+            const u32 peers = __match_any_sync(0xffffffffu, d2);
+            if (d2 < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&S.nh[d2], __popc(peers));
+        }
+    }
+    if (nslot >= 0) {
+        __syncthreads();
+        if (S.nh[tid]) atomicAdd(&a.lhist[nslot * 256 + tid], S.nh[tid]);
+    }
+}
+
+// ---- segmentation of the sorted keys
+// Positions are handled in tiles of SEG_TILE; warp w of a tile owns the SEG_IPT * 32 consecutive positions starting at
+// tile base + w * 32 * SEG_IPT and visits them lane-striped (position = chunk base + j * 32 + lane), so every load is
+// coalesced. Group starts are kept as a bitmask (bit p of the mask: a group starts at position p), written by the
+// count kernel into the free half of the key ping-pong; the emit kernels read only the bits.
+__device__ __forceinline__ u32 lsd_final_par(const Ctl *c) { return __popc(active_slots(c)) & 1; }
+
+struct SegBufs {
+    const u64 *key;
+    const u32 *val, *hi;
+    u32 *bits;          // start bitmask (free key buffer)
+    u32 *gbase, *gidx;  // per group start: list slot base, list index | GRP_LARGE (free value / block buffers)
+    bool has_hi;
+    u32 m;
+};
+__device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
+    const Ctl *c = a.ctl;
+    const u32 par = lsd_final_par(c);
+    SegBufs v;
+    v.key = a.lkey[par]; v.val = a.lval[par]; v.hi = a.lhi[par];
+    v.bits = reinterpret_cast<u32 *>(a.lkey[par ^ 1]);
+    v.gbase = a.lval[par ^ 1];
+    v.gidx = a.lhi[par ^ 1];
+    v.has_hi = lsd_has_hi(a);
+    v.m = c->m;
+    return v;
+}
+constexpr u32 GRP_LARGE = 0x80000000u;
+constexpr u32 SEG_WORDS = SEG_IPT;  // mask words per warp chunk
+
+// Per tile: start bits and the tile's last group start (position 0 always starts a group).
+__global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
+    __shared__ u32 ws[TPB / 32];
+    const SegBufs v = seg_bufs(a);
+    const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
+    const u32 lane = lane_id(), warp = warp_id();
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
+        u32 last = 0;
+#pragma unroll 4
+        for (int j = 0; j < SEG_IPT; j++) {
+            const u32 p = cb + j * 32 + lane;
+            const bool ok = p < v.m;
+            u64 k = ok ? v.key[p] : 0ull;
+            u32 h = ok && v.has_hi ? v.hi[p] : 0u;
+            u64 kp = __shfl_up_sync(0xffffffffu, k, 1);
+            u32 hp = __shfl_up_sync(0xffffffffu, h, 1);
+            if (lane == 0 && ok && p > 0) { kp = v.key[p - 1]; hp = v.has_hi ? v.hi[p - 1] : 0u; }
+            const bool st = ok && (p == 0 || k != kp || h != hp);
+            const u32 b = __ballot_sync(0xffffffffu, st);
+            if (lane == 0 && cb + j * 32 < v.m) v.bits[(cb >> 5) + j] = b;
+            if (st) last = p;
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+        if (lane == 0) ws[warp] = last;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 tl = 0;
+            for (int w = 0; w < TPB / 32; w++) tl = max(tl, ws[w]);
+            a.segagg[(u64)t * 2] = tl;
+        }
+        __syncthreads();
+    }
+}
+
+// Exclusive max-scan of the tiles' last starts (one CTA): the start of the group open at each tile's first position.
+__global__ void __launch_bounds__(1024) k_seg_scan(FwdArgs a) {
+    __shared__ u32 ws[33];
+    __shared__ u32 prev[1024];
+    const u32 m = a.ctl->m;
+    const u32 ntiles = (m + SEG_TILE - 1) / SEG_TILE;
+    u32 carry = 0;
+    for (u32 t0 = 0; t0 < ntiles; t0 += 1024) {
+        const u32 t = t0 + threadIdx.x;
+        const u32 l = t < ntiles ? a.segagg[(u64)t * 2] : 0u;
+        const u32 il = block_incl_max<1024>(l, ws);
+        prev[threadIdx.x] = il;
+        __syncthreads();
+        if (t < ntiles) a.segagg[(u64)t * 2 + 1] = max(carry, threadIdx.x ? prev[threadIdx.x - 1] : 0u);
+        carry = max(carry, prev[1023]);
+        __syncthreads();
+    }
+}
+
+// The warp's view of its chunk: the mask words (lane j holds word j), and the start of the group open at the chunk's
+// first position.
+struct SegChunk {
+    u32 cb, word, nextw, carry0;
+};
+__device__ __forceinline__ SegChunk seg_chunk(const FwdArgs &a, const SegBufs &v, u32 t, u32 *wl) {
+    const u32 lane = lane_id(), warp = warp_id();
+    SegChunk c;
+    c.cb = t * SEG_TILE + warp * 32 * SEG_IPT;
+    const u32 w0 = c.cb >> 5;
+    const u32 nw = (v.m + 31) >> 5;
+    c.word = lane < SEG_WORDS && w0 + lane < nw ? v.bits[w0 + lane] : 0u;
+    // bit 0 of the word after the chunk: the start flag of the first position past it
+    c.nextw = w0 + SEG_WORDS < nw ? v.bits[w0 + SEG_WORDS] : 1u;
+    u32 last = 0;
+    if (lane < SEG_WORDS && c.word) last = c.cb + lane * 32 + 31 - __clz(c.word);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+    if (lane == 0) wl[warp] = last;
+    __syncthreads();
+    u32 cr = a.segagg[(u64)t * 2 + 1];
+    for (u32 w = 0; w < warp; w++) cr = max(cr, wl[w]);
+    c.carry0 = cr;
+    return c;
+}
+// Position j * 32 + lane of the chunk: start / end flags and the group's first position (carry: running start).
+__device__ __forceinline__ void seg_step(const SegBufs &v, const SegChunk &c, int j, u32 &carry, u32 &p, bool &valid,
+                                         bool &st, bool &en, u32 &gfirst) {
+    const u32 lane = lane_id();
+    const u32 w = __shfl_sync(0xffffffffu, c.word, j);
+    const u32 wn = j + 1 < SEG_IPT ? __shfl_sync(0xffffffffu, c.word, (j + 1) & 31) : c.nextw;
+    p = c.cb + j * 32 + lane;
+    valid = p < v.m;
+    st = (w >> lane) & 1;
+    en = p + 1 >= v.m || (lane < 31 ? (w >> (lane + 1)) & 1 : wn & 1);
+    const u32 x = warp_incl_max(valid && st ? p : 0u);
+    gfirst = max(carry, x);
+    carry = __shfl_sync(0xffffffffu, gfirst, 31);
+}
+
+// Block-wide exclusive sum of a 64-bit value (TPB threads); contains __syncthreads().
+__device__ __forceinline__ u64 block_excl_sum64(u64 v, u64 *ws, u64 *total) {
+    u64 inc = v;
+    const u32 lane = lane_id(), warp = warp_id();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u64 t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (u32)o) inc += t;
+    }
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    u64 before = 0, tot = 0;
+    for (u32 w = 0; w < TPB / 32; w++) {
+        const u64 x = ws[w];
+        if (w < warp) before += x;
+        tot += x;
+    }
+    __syncthreads();
+    *total = tot;
+    return before + inc - v;
+}
+
+// Emit, part 1 (group ends): groups of one resolve; every other group takes its slots in the next small-group list
+// (<= SMAX) or large-group list, writes its descriptor and tile-map entries, and records its slot base and index at
+// its first position for part 2. Slots are allocated once per tile (a count pass, a block scan, one atomic per list).
+__global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
+    __shared__ u32 wl[TPB / 32];
+    __shared__ u64 ws[2][TPB / 32];
+    __shared__ u64 base[3];
+    Ctl *c = a.ctl;
+    const SegBufs v = seg_bufs(a);
+    const u32 rpar = c->rpar, round = c->round;
+    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)];
+    const ListView res = a.lists[L_R0 + rpar];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
+    const u32 TS = a.smax;
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SegChunk ch = seg_chunk(a, v, t, wl);
+        // count: singles | small groups << 16 | small elements << 32 ; large groups | large elements << 32
+        u64 cs = 0, cl = 0;
+        {
+            u32 carry = ch.carry0;
+            for (int j = 0; j < SEG_IPT; j++) {
+                u32 p, gf; bool ok, st, en;
+                seg_step(v, ch, j, carry, p, ok, st, en, gf);
+                if (!ok || !en) continue;
+                const u32 len = p - gf + 1;
+                if (len == 1) cs += 1;
+                else if (len <= TS) cs += (1ull << 16) | ((u64)len << 32);
+                else cl += 1ull | ((u64)len << 32);
+            }
+        }
+        u64 ts, tl;
+        u64 xs = block_excl_sum64(cs, ws[0], &ts);
+        u64 xl = block_excl_sum64(cl, ws[1], &tl);
+        if (threadIdx.x == 0) {
+            base[0] = (ts & 0xFFFF) ? atomicAdd(&c->cnt[L_R0 + rpar], ts & 0xFFFF) : 0ull;
+            base[1] = (ts >> 16) & 0xFFFF ? atomicAdd(&c->cnt[L_S0 + (rpar ^ 1)], (((ts >> 16) & 0xFFFF) << 32) | (ts >> 32)) : 0ull;
+            base[2] = (u32)tl ? atomicAdd(&c->cnt[L_L0 + (rpar ^ 1)], (tl << 32) | (tl >> 32)) : 0ull;
+        }
+        __syncthreads();
+        u32 r1 = (u32)base[0] + (u32)(xs & 0xFFFF);
+        u32 sidx = (u32)(base[1] >> 32) + (u32)((xs >> 16) & 0xFFFF), se = (u32)base[1] + (u32)(xs >> 32);
+        u32 lidx = (u32)(base[2] >> 32) + (u32)xl, le = (u32)base[2] + (u32)(xl >> 32);
+        u32 carry = ch.carry0;
+        for (int j = 0; j < SEG_IPT; j++) {
+            u32 p, gf; bool ok, st, en;
+            seg_step(v, ch, j, carry, p, ok, st, en, gf);
+            if (!ok || !en) continue;
+            const u32 len = p - gf + 1;
+            const u32 b = v.has_hi ? v.hi[p] : 0u;
+            const u32 head = gf - a.blk[b].soff;
+            if (len == 1) {
+                resolve(a, isa_nxt, v.val[p], head, b, res, r1++);
+                continue;
+            }
+            Seg g;
+            g.len = len; g.head = head; g.bd = b;
+            if (len <= TS) {
+                g.start = se;
+                KGB_GUARD(sidx < a.cap_segs && (u64)se + len <= a.cap_n, &c->err, E_SEG) {
+                    sl.seg[sidx] = g;
+                    write_tmap_small(a, sl.tmap, TS, se, len, sidx);
+                    if (len > WARP_GROUP) sl.tbig[se / TS] = round + 1;
+                    v.gbase[gf] = se;
+                    v.gidx[gf] = sidx;
+                }
+                sidx++; se += len;
+            } else {
+                g.start = le;
+                KGB_GUARD(lidx < a.cap_segl && (u64)le + len <= a.cap_n, &c->err, E_SEG) {
+                    ll.seg[lidx] = g;
+                    v.gbase[gf] = le;
+                    v.gidx[gf] = lidx | GRP_LARGE;
+                }
+                lidx++; le += len;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Emit, part 2 (every suffix of a group of two or more): its rank (the group's first position), its slot in its
+// group's list, and for large groups the bucket-pass tile map (the suffix at a multiple of TSM names its group).
+__global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
+    __shared__ u32 wl[TPB / 32];
+    Ctl *c = a.ctl;
+    const SegBufs v = seg_bufs(a);
+    const u32 rpar = c->rpar;
+    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SegChunk ch = seg_chunk(a, v, t, wl);
+        u32 carry = ch.carry0;
+        for (int j = 0; j < SEG_IPT; j++) {
+            u32 p, gf; bool ok, st, en;
+            seg_step(v, ch, j, carry, p, ok, st, en, gf);
+            if (!ok || (st && en)) continue;  // groups of one were resolved by part 1
+            const u32 b = v.has_hi ? v.hi[p] : 0u;
+            const u32 id = v.val[p];
+            const u32 head = gf - a.blk[b].soff;
+            const u32 gi = v.gidx[gf];
+            const u32 slot = v.gbase[gf] + (p - gf);
+            KGB_GUARD(id < a.cap_n && slot < a.cap_n, &c->err, E_LIST) {
+                isa_nxt[id] = head;
+                if (gi & GRP_LARGE) {
+                    ll.eid[slot] = id;
+                    if (slot % TSM == 0) {
+                        KGB_GUARD(slot / TSM < a.cap_tml, &c->err, E_TMAP) ll.tmap[slot / TSM] = gi & ~GRP_LARGE;
+                    }
+                } else {
+                    sl.eid[slot] = id;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}

@@ -40,6 +40,7 @@ class Prof(ctypes.Structure):
 PLAIN = 1
 OPT_SMALL_GROUP = 1
 OPT_WARP_PATH = 2
+OPT_LSD_ROUND0 = 3
 
 _lib = None
 

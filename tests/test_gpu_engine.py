@@ -85,3 +85,38 @@ def test_engine_configs_give_identical_results():
         if ref is None:
             ref = got
         assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+
+
+@pytest.mark.parametrize("lsd_round0", [0, 1])
+def test_round0_paths_on_mixed_batch(lsd_round0):
+    """Round 0 as one LSD radix sort of the batch, or as bucket passes + tiles: both must give the oracle's L column
+    and sampled indexes, on a batch that mixes two-byte blocks (the engine's minimum), runs longer than a tile (large groups spanning
+    segmentation tiles) and ordinary text."""
+    import torch
+
+    texts = [np.array([7, 1], np.uint8), np.array([3, 3], np.uint8), np.full(20_000, 97, np.uint8),
+             W.periodic(60_000, 11, 7, 1 << 14), W.markov2(90_000, 12), W.test_block(5, 5_000),
+             np.zeros(3_000, np.uint8), W.zipf_prose(150_000, 13)]
+    buf, offs = _pack(texts)
+    r = 1 << 10
+    iouts, k = [], 0
+    for t in texts:
+        iouts.append(k)
+        k += (t.size - 1) // r + 1
+    dT = torch.from_numpy(buf).cuda()
+    dL = torch.zeros(buf.size + len(texts), dtype=torch.uint8, device="cuda")
+    dI = torch.zeros(k, dtype=torch.int32, device="cuda")
+    eng = codec.Engine()
+    eng.config(lsd_round0=lsd_round0)
+    blocks = [(off, t.size, r, io) for t, off, io in zip(texts, offs, iouts)]
+    for _ in range(2):  # the second call reuses the captured graph and the look-back words of the first
+        assert eng.fwd(dT, dL, dI, blocks) == 0
+        assert eng.wait()[0] == 0
+        L = dL.cpu().numpy()
+        I = dI.cpu().numpy()
+        for b, (t, off, io) in enumerate(zip(texts, offs, iouts)):
+            oU, oI = O.bwt_aux(t, r)[1:]
+            assert np.array_equal(I[io:io + oI.size], oI), b
+            col = L[off + b: off + b + t.size + 1]
+            p0 = int(oI[0])
+            assert np.array_equal(np.concatenate([col[:p0], col[p0 + 1:]]), oU), b
