@@ -38,6 +38,7 @@ constexpr int TSM = 2048;  // elements per tile of the bucket passes
 constexpr int IPM = TSM / TPB;
 constexpr u32 DEPTH_PREFIX = 8, DEPTH_RANK = 4;
 constexpr u32 WARP_GROUP = 32;  // groups up to this long are handled by one warp (k_tile_warp)
+constexpr u32 GTINY = 8;        // groups up to this long leave the rank rounds' tile lists for one thread each
 // Seg.bd flag of small groups: the group came from the previous round's small-group list and passed that round
 // unsplit, so both rank buffers already hold its head (set only on groups whose input was a small-group list: a group
 // cut out of a larger one by the bucket passes has its parent's head in the other buffer).
@@ -63,19 +64,23 @@ struct FwdArgs {
     u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
-    u64 *lkey[2];
-    u32 *lval[2], *lhi[2];
+    u32 *lval[2], *lhi[2], *segbits;
     u64 *lstat;
     u32 *lhist, *ltile, *segagg;
     u32 spin_limit;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
-    u64 cap_n, cap_segs, cap_segl, cap_tms, cap_tml;
+    u64 cap_n, cap_segs, cap_segl, cap_segt, cap_tms, cap_tml;
 };
 
 // device error bits
 enum : u32 { E_ROUNDS = 1, E_PASSES = 2, E_TILE = 4, E_LIST = 8, E_SEG = 16, E_TMAP = 32, E_RANK = 64, E_HIST = 128 };
 
 __device__ __forceinline__ u32 seg_blk(u32 bd) { return bd & 0xFFFFFFu; }
+// End (exclusive text offset) of block b.
+__device__ __forceinline__ u64 blk_end(const FwdArgs &a, u32 b) {
+    const BlockInfo B = a.blk[b];
+    return (u64)B.off + B.n;
+}
 __device__ __forceinline__ u32 seg_depth(u32 bd) { return bd >> 24; }
 
 // Depth of the first bucket pass of a rank-round group from the OR/AND of its keys: the byte of the highest
@@ -132,6 +137,7 @@ struct TileSmem {
     u32 ws2[TPB / 32 + 1];
     u64 red[4][TPB / 32];
     u32 bases[4];
+    u32 pbases[2];
 };
 
 __device__ __forceinline__ void write_tmap_small(const FwdArgs &a, u32 *tmap, u32 ts, u32 start, u32 len, u32 sidx) {
@@ -348,7 +354,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
 
         // ---- split groups: blocked arrangement x = tid * IPT + j
         u32 st[IPT], en[IPT];
-        u32 gl = 0, ns = 0, ng = 0;
+        u32 gl = 0;
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
             const u32 x = tid * IPT + j;
@@ -360,9 +366,6 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 en[j] = x + 1 == S.lstart[sj + 1] || kx != S.klo[x + 1];
                 if (st[j]) gl = x;
                 if (st[j] && x != S.lstart[sj]) atomicOr(&S.lhead[sj], 0x80000000u);  // the group splits
-                const u32 surv = !(st[j] && en[j]);
-                ns += surv;
-                ng += surv && st[j];
             }
         }
         // group first member: inclusive max-scan of group starts (gl = last start in this thread, or 0)
@@ -377,19 +380,55 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             carry = tid ? prevmax[tid - 1] : 0u;
             __syncthreads();
         }
-        u32 tot_pack = 0;
-        const u32 pre = block_excl_sum<TPB>(ns | (ng << 16), S.ws, &tot_pack);
-        const u32 tot_s = tot_pack & 0xFFFFu, tot_g = tot_pack >> 16;
-        if (tid == 0) {
-            atomicAdd(&a.ctl->tile_elems[0], (u64)cnt);
-            const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)tot_g << 32) | tot_s);
-            S.bases[0] = (u32)o;
-            S.bases[1] = (u32)(o >> 32);
-            S.bases[2] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)(cnt - tot_s));
+        // run lengths at the runs' first positions (the keys are no longer needed)
+        {
+            u32 gf = carry;
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = tid * IPT + j;
+                if (x >= cnt) break;
+                if (st[j]) gf = x;
+                if (en[j]) S.klo[gf] = (KeyT)(x - gf + 1);
+            }
         }
         __syncthreads();
+        // survivors and runs per destination: tiny runs (<= GTINY) to the tiny list, longer ones to the small list
+        u32 ns = 0, ng = 0, np = 0, ngp = 0;
+        {
+            u32 gf = carry;
+#pragma unroll
+            for (int j = 0; j < IPT; j++) {
+                const u32 x = tid * IPT + j;
+                if (x >= cnt) break;
+                if (st[j]) gf = x;
+                if (st[j] && en[j]) continue;
+                if ((u32)S.klo[gf] <= GTINY) { np++; ngp += st[j]; } else { ns++; ng += st[j]; }
+            }
+        }
+        u32 tot_pack = 0, tot_packp = 0;
+        const u32 pre = block_excl_sum<TPB>(ns | (ng << 16), S.ws, &tot_pack);
+        const u32 prep = block_excl_sum<TPB>(np | (ngp << 16), S.ws, &tot_packp);
+        const u32 tot_s = tot_pack & 0xFFFFu, tot_g = tot_pack >> 16;
+        const u32 tot_p = tot_packp & 0xFFFFu, tot_gp = tot_packp >> 16;
+        if (tid == 0) {
+            atomicAdd(&a.ctl->tile_elems[0], (u64)cnt);
+            if (tot_s) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)tot_g << 32) | tot_s);
+                S.bases[0] = (u32)o;
+                S.bases[1] = (u32)(o >> 32);
+            }
+            if (tot_p) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)tot_gp << 32) | tot_p);
+                S.pbases[0] = (u32)o;
+                S.pbases[1] = (u32)(o >> 32);
+            }
+            S.bases[2] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)(cnt - tot_s - tot_p));
+        }
+        __syncthreads();
+        const ListView outp = a.lists[L_P0 + (rpar ^ 1)];
         const u32 ebase = S.bases[0], sbase = S.bases[1], rbase = S.bases[2];
-        u32 es = pre & 0xFFFFu, gs = pre >> 16;
+        const u32 pebase = S.pbases[0], psbase = S.pbases[1];
+        u32 es = pre & 0xFFFFu, gs = pre >> 16, ep = prep & 0xFFFFu, gp = prep >> 16;
         u32 gfirst = carry;
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
@@ -401,21 +440,34 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             const u32 lh = S.lhead[sj], bd = S.lblk[sj];
             const bool unsplit = !(lh >> 31);
             if (st[j] && en[j]) {
-                resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + (x - es));
-            } else {
-                const u32 head = (lh & 0x7FFFFFFFu) + (gfirst - s0);
-                // a group that passed the previous round unsplit and passes this one unsplit already has this head
-                // in the write buffer (written two rounds ago)
-                if (!((bd & STABLE) && unsplit)) {
-                    KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+                // finished suffixes take the resolved slots in position order after the survivors before them
+                resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + (x - es - ep));
+                continue;
+            }
+            const u32 head = (lh & 0x7FFFFFFFu) + (gfirst - s0);
+            // a group that passed the previous round unsplit and passes this one unsplit already has this head
+            // in the write buffer (written two rounds ago)
+            if (!((bd & STABLE) && unsplit)) {
+                KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+            }
+            const u32 len = (u32)S.klo[gfirst];
+            const u32 sbd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
+            if (len <= GTINY) {
+                KGB_GUARD(pebase + ep < a.cap_n, &a.ctl->err, E_LIST) outp.eid[pebase + ep] = id;
+                if (st[j]) gp++;
+                if (en[j]) {
+                    Seg g;
+                    g.start = pebase + ep + 1 - len; g.len = len; g.head = head; g.bd = sbd;
+                    KGB_GUARD(psbase + gp - 1 < a.cap_segt, &a.ctl->err, E_SEG) outp.seg[psbase + gp - 1] = g;
                 }
+                ep++;
+            } else {
                 KGB_GUARD(ebase + es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + es] = id;
                 if (st[j]) gs++;
                 if (en[j]) {
-                    const u32 len = x - gfirst + 1, sidx = sbase + gs - 1, start = ebase + es + 1 - len;
+                    const u32 sidx = sbase + gs - 1, start = ebase + es + 1 - len;
                     Seg g;
-                    g.start = start; g.len = len; g.head = head;
-                    g.bd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
+                    g.start = start; g.len = len; g.head = head; g.bd = sbd;
                     KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
                     write_tmap_small(a, out.tmap, TS, start, len, sidx);
                     if (len > WARP_GROUP) out.tbig[start / TS] = ctl->round + 1;
@@ -579,38 +631,70 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
             S.key[1][d] = kx; S.val[1][d] = S.val[0][x]; S.sg[1][d] = (u16)sj;
         }
         __syncwarp();
-        // ---- count survivors, groups, finished suffixes; mark segments that split
-        u32 ns = 0, ng = 0;
-        for (u32 xb = X0; xb < X1; xb += 32) {
-            const u32 x = xb + lane;
-            bool st = false, en = false;
-            if (x < X1) {
-                const u32 sj = S.sg[1][x];
-                const KeyT kx = S.key[1][x];
-                st = x == S.lstart[sj] || kx != S.key[1][x - 1];
-                en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
-                if (st && x != S.lstart[sj]) atomicOr(&S.lhead[sj], 0x80000000u);
+        // ---- mark segments that split; run lengths at the runs' first positions (buffer 0 is free)
+        {
+            u32 carry = X0;
+            for (u32 xb = X0; xb < X1; xb += 32) {
+                const u32 x = xb + lane;
+                bool st = false, en = false;
+                if (x < X1) {
+                    const u32 sj = S.sg[1][x];
+                    const KeyT kx = S.key[1][x];
+                    st = x == S.lstart[sj] || kx != S.key[1][x - 1];
+                    en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
+                    if (st && x != S.lstart[sj]) atomicOr(&S.lhead[sj], 0x80000000u);
+                }
+                const u32 gfirst = max(carry, warp_incl_max(x < X1 && st ? x : 0u));
+                if (x < X1 && en) S.key[0][gfirst] = (KeyT)(x - gfirst + 1);
+                carry = __shfl_sync(0xffffffffu, gfirst, 31);
             }
-            const bool surv = x < X1 && !(st && en);
-            ns += __popc(__ballot_sync(0xffffffffu, surv));
-            ng += __popc(__ballot_sync(0xffffffffu, surv && st));
         }
-        const u32 nres = (X1 - X0) - ns;
-        u32 ebase = 0, sbase = 0, rbase = 0;
+        __syncwarp();
+        // ---- count survivors and runs per destination (tiny runs to the tiny list), finished suffixes
+        u32 ns = 0, ng = 0, np = 0, ngp = 0;
+        {
+            u32 carry = X0;
+            for (u32 xb = X0; xb < X1; xb += 32) {
+                const u32 x = xb + lane;
+                bool st = false, en = false;
+                if (x < X1) {
+                    const u32 sj = S.sg[1][x];
+                    const KeyT kx = S.key[1][x];
+                    st = x == S.lstart[sj] || kx != S.key[1][x - 1];
+                    en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
+                }
+                const u32 gfirst = max(carry, warp_incl_max(x < X1 && st ? x : 0u));
+                carry = __shfl_sync(0xffffffffu, gfirst, 31);
+                const bool surv = x < X1 && !(st && en);
+                const bool tiny = surv && (u32)S.key[0][gfirst] <= GTINY;
+                ns += __popc(__ballot_sync(0xffffffffu, surv && !tiny));
+                ng += __popc(__ballot_sync(0xffffffffu, surv && !tiny && st));
+                np += __popc(__ballot_sync(0xffffffffu, tiny));
+                ngp += __popc(__ballot_sync(0xffffffffu, tiny && st));
+            }
+        }
+        const u32 nres = (X1 - X0) - ns - np;
+        u32 ebase = 0, sbase = 0, rbase = 0, pebase = 0, psbase = 0;
         if (lane == 0) {
             atomicAdd(&a.ctl->tile_elems[1], (u64)(X1 - X0));
             if (ns) {
                 const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)ng << 32) | ns);
                 ebase = (u32)o; sbase = (u32)(o >> 32);
             }
+            if (np) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)ngp << 32) | np);
+                pebase = (u32)o; psbase = (u32)(o >> 32);
+            }
             if (nres) rbase = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)nres);
         }
         ebase = __shfl_sync(0xffffffffu, ebase, 0);
         sbase = __shfl_sync(0xffffffffu, sbase, 0);
         rbase = __shfl_sync(0xffffffffu, rbase, 0);
-        __syncwarp();
+        pebase = __shfl_sync(0xffffffffu, pebase, 0);
+        psbase = __shfl_sync(0xffffffffu, psbase, 0);
+        const ListView outp = a.lists[L_P0 + (rpar ^ 1)];
         // ---- emit
-        u32 es = 0, gs = 0, rs = 0, carry = X0;  // running counts; carry: start of the open group
+        u32 es = 0, gs = 0, ep = 0, gp = 0, rs = 0, carry = X0;  // running counts; carry: start of the open run
         for (u32 xb = X0; xb < X1; xb += 32) {
             const u32 x = xb + lane;
             const bool valid = x < X1;
@@ -622,12 +706,16 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
                 st = x == S.lstart[sj] || kx != S.key[1][x - 1];
                 en = x + 1 == S.lstart[sj + 1] || kx != S.key[1][x + 1];
             }
-            const bool single = valid && st && en, surv = valid && !(st && en);
-            const u32 b_surv = __ballot_sync(0xffffffffu, surv), b_gs = __ballot_sync(0xffffffffu, surv && st);
-            const u32 b_one = __ballot_sync(0xffffffffu, single);
             const u32 gf = warp_incl_max(valid && st ? x : 0u);
             const u32 gfirst = max(gf, carry);
-            const u32 my_es = es + __popc(b_surv & lt_mask), my_gs = gs + __popc(b_gs & lt_mask);
+            const bool single = valid && st && en, surv = valid && !(st && en);
+            const u32 len = surv ? (u32)S.key[0][gfirst] : 0u;
+            const bool tiny = surv && len <= GTINY, smallg = surv && len > GTINY;
+            const u32 b_s = __ballot_sync(0xffffffffu, smallg), b_gs = __ballot_sync(0xffffffffu, smallg && st);
+            const u32 b_p = __ballot_sync(0xffffffffu, tiny), b_gp = __ballot_sync(0xffffffffu, tiny && st);
+            const u32 b_one = __ballot_sync(0xffffffffu, single);
+            const u32 my_es = es + __popc(b_s & lt_mask), my_gs = gs + __popc(b_gs & lt_mask);
+            const u32 my_ep = ep + __popc(b_p & lt_mask), my_gp = gp + __popc(b_gp & lt_mask);
             const u32 my_rs = rs + __popc(b_one & lt_mask);
             if (valid) {
                 const u32 id = S.val[1][x], s0 = S.lstart[sj], lh = S.lhead[sj], bd = S.lbd[sj];
@@ -639,25 +727,150 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
                     if (!((bd & STABLE) && unsplit)) {
                         KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
                     }
-                    KGB_GUARD(ebase + my_es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + my_es] = id;
-                    if (en) {
-                        const u32 len = x - gfirst + 1, sidx = sbase + my_gs + (st ? 1u : 0u) - 1u;
-                        const u32 start = ebase + my_es + 1 - len;
-                        Seg g;
-                        g.start = start; g.len = len; g.head = head;
-                        g.bd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
-                        KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
-                        write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                    const u32 sbd = seg_blk(bd) | (!PREFIX && !KEYED && unsplit ? STABLE : 0u);
+                    if (tiny) {
+                        KGB_GUARD(pebase + my_ep < a.cap_n, &a.ctl->err, E_LIST) outp.eid[pebase + my_ep] = id;
+                        if (en) {
+                            const u32 sidx = psbase + my_gp + (st ? 1u : 0u) - 1u;
+                            Seg g;
+                            g.start = pebase + my_ep + 1 - len; g.len = len; g.head = head; g.bd = sbd;
+                            KGB_GUARD(sidx < a.cap_segt, &a.ctl->err, E_SEG) outp.seg[sidx] = g;
+                        }
+                    } else {
+                        KGB_GUARD(ebase + my_es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + my_es] = id;
+                        if (en) {
+                            const u32 sidx = sbase + my_gs + (st ? 1u : 0u) - 1u;
+                            const u32 start = ebase + my_es + 1 - len;
+                            Seg g;
+                            g.start = start; g.len = len; g.head = head; g.bd = sbd;
+                            KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
+                            write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                        }
                     }
                 }
             }
-            es += __popc(b_surv);
+            es += __popc(b_s);
             gs += __popc(b_gs);
+            ep += __popc(b_p);
+            gp += __popc(b_gp);
             rs += __popc(b_one);
             carry = __shfl_sync(0xffffffffu, gfirst, 31);
         }
     }
 }
+
+// ------------------------------------------------------------------------------------------------ tiny groups
+// Rank rounds: one thread per group of at most GTINY suffixes. The thread gathers the group's keys into registers,
+// sorts them with a sorting network (2, 4 or 8 inputs, the widest group of the warp decides), and emits ranks,
+// finished suffixes and the surviving runs, which are tiny again; allocations are aggregated per warp.
+
+__device__ __forceinline__ void cswap(u32 &ka, u32 &va, u32 &kb, u32 &vb) {
+    const bool sw = kb < ka;
+    const u32 tk = sw ? kb : ka, tv = sw ? vb : va;
+    kb = sw ? ka : kb;
+    vb = sw ? va : vb;
+    ka = tk;
+    va = tv;
+}
+#define KGB_CS(i, j) cswap(k[i], v[i], k[j], v[j])
+
+__global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h;
+    const ListView in = a.lists[L_P0 + rpar], out = a.lists[L_P0 + (rpar ^ 1)], res = a.lists[L_R0 + rpar];
+    const u64 c = ctl->cnt[L_P0 + rpar];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segt) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 *isa_cur = a.isa[rpar];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 lane = lane_id();
+    for (u32 base = blockIdx.x * TPB; base < nseg; base += gridDim.x * TPB) {
+        const u32 s = base + threadIdx.x;
+        const bool ok = s < nseg;
+        Seg g = {0, 0, 0, 0};
+        if (ok) g = in.seg[s];
+        u32 len = g.len;
+        if (len > GTINY || (u64)g.start + len > nelem) {  // broken list invariant: report, never overrun
+            atomicOr(&a.ctl->err, E_SEG);
+            len = 0;
+        }
+        const u32 b = seg_blk(g.bd);
+        const u64 end = len ? blk_end(a, b) : 0;
+        u32 k[GTINY], v[GTINY];
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? in.eid[g.start + q] : 0u;
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) k[q] = q < len ? rank_key(isa_cur, v[q], h, end) : 0xFFFFFFFFu;
+        const u32 mlen = __reduce_max_sync(0xffffffffu, len);
+        if (mlen <= 2) {
+            KGB_CS(0, 1);
+        } else if (mlen <= 4) {
+            KGB_CS(0, 1); KGB_CS(2, 3); KGB_CS(0, 2); KGB_CS(1, 3); KGB_CS(1, 2);
+        } else {
+            KGB_CS(0, 1); KGB_CS(2, 3); KGB_CS(4, 5); KGB_CS(6, 7);
+            KGB_CS(0, 2); KGB_CS(1, 3); KGB_CS(4, 6); KGB_CS(5, 7);
+            KGB_CS(1, 2); KGB_CS(5, 6);
+            KGB_CS(0, 4); KGB_CS(1, 5); KGB_CS(2, 6); KGB_CS(3, 7);
+            KGB_CS(2, 4); KGB_CS(3, 5);
+            KGB_CS(1, 2); KGB_CS(3, 4); KGB_CS(5, 6);
+        }
+        // runs of equal keys: survivors (runs of two or more), their runs, finished suffixes
+        u32 ns = 0, ng = 0, n1 = 0;
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            if (q >= len) break;
+            const bool st = q == 0 || k[q] != k[q - 1];
+            const bool en = q + 1 == len || k[q] != k[q + 1];
+            if (st && en) n1++;
+            else { ns++; ng += st; }
+        }
+        const bool unsplit = ng == 1 && ns == len;  // one run covers the group
+        const u32 pk = ns | (ng << 10) | (n1 << 20);  // each at most GTINY per thread: warp totals <= 256
+        const u32 incl = warp_incl_sum(pk), tot = __shfl_sync(0xffffffffu, incl, 31), excl = incl - pk;
+        u32 ebase = 0, sbase = 0, rbase = 0;
+        if (lane == 0) {
+            const u32 ts = tot & 0x3FF, tg = (tot >> 10) & 0x3FF, t1 = tot >> 20;
+            if (ts) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)tg << 32) | ts);
+                ebase = (u32)o; sbase = (u32)(o >> 32);
+            }
+            if (t1) rbase = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)t1);
+        }
+        u32 e = __shfl_sync(0xffffffffu, ebase, 0) + (excl & 0x3FF);
+        u32 gi = __shfl_sync(0xffffffffu, sbase, 0) + ((excl >> 10) & 0x3FF);
+        u32 r = __shfl_sync(0xffffffffu, rbase, 0) + (excl >> 20);
+        const bool skip_rank = (g.bd & STABLE) && unsplit;
+        u32 rs = 0;  // first position of the current run
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            if (q >= len) break;
+            const bool st = q == 0 || k[q] != k[q - 1];
+            const bool en = q + 1 == len || k[q] != k[q + 1];
+            if (st) rs = q;
+            if (st && en) {
+                resolve(a, isa_nxt, v[q], g.head + q, b, res, r++);
+                continue;
+            }
+            const u32 head = g.head + rs;
+            if (!skip_rank) {
+                KGB_GUARD(v[q] < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[v[q]] = head;
+            }
+            KGB_GUARD(e < a.cap_n, &a.ctl->err, E_LIST) out.eid[e] = v[q];
+            e++;
+            if (en) {
+                Seg ng_;
+                ng_.len = q - rs + 1; ng_.start = e - ng_.len; ng_.head = head;
+                ng_.bd = b | (unsplit ? STABLE : 0u);
+                KGB_GUARD(gi < a.cap_segt, &a.ctl->err, E_SEG) out.seg[gi] = ng_;
+                gi++;
+            }
+        }
+    }
+}
+#undef KGB_CS
 
 // ------------------------------------------------------------------------------------------------ bucket passes
 // Work lists of large groups are tiled by TSM elements; every group is longer than TSM, so a tile meets at most
@@ -1051,9 +1264,10 @@ __global__ void k_ctl_msd_next(FwdArgs a) {
 __global__ void k_ctl_round_end(FwdArgs a) {
     Ctl *c = a.ctl;
     const u32 rp = c->rpar;
-    const u32 active = elems(c, L_S0 + (rp ^ 1)) + elems(c, L_L0 + (rp ^ 1));
+    const u32 active = elems(c, L_S0 + (rp ^ 1)) + elems(c, L_L0 + (rp ^ 1)) + elems(c, L_P0 + (rp ^ 1));
     c->cnt[L_S0 + rp] = 0;
     c->cnt[L_L0 + rp] = 0;
+    c->cnt[L_P0 + rp] = 0;
     c->cnt[L_KS] = 0;
     c->cnt[L_K0] = 0;
     c->cnt[L_K1] = 0;
@@ -1146,6 +1360,11 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
         add((void **)&lists[l].eid, n * 4);
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
+        const bool tiny = l == L_P0 || l == L_P1;
+        if (tiny) {  // ids and segment descriptors only
+            add((void **)&lists[l].seg, nseg_small * sizeof(Seg));
+            continue;
+        }
         if (l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
         if (!res) {
             add((void **)&lists[l].seg, (small ? nseg_small : nseg_large) * sizeof(Seg));
@@ -1161,11 +1380,11 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     add((void **)&d_orand64, nseg_large * 16);
     const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
     for (int q = 0; q < 2; q++) {
-        add((void **)&d_lkey[q], n * 8);
         add((void **)&d_lval[q], n * 4);
         add((void **)&d_lhi[q], n * 4);
     }
     add((void **)&d_lstat, ltiles * 256 * 8);
+    add((void **)&d_segbits, n / 8 + 64);
     add((void **)&d_lhist, NSLOT * 256 * 4);
     add((void **)&d_ltile, 64);
     add((void **)&d_segagg, stiles * 8 * 4);
@@ -1198,7 +1417,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     Bcap = bcap;
     Icap = icap;
     sa_cap = want_sa;
-    cap_segs = nseg_small; cap_segl = nseg_large; cap_tms = ntm_small; cap_tml = ntm_large;
+    cap_segs = nseg_small; cap_segl = nseg_large; cap_segt = nseg_small; cap_tms = ntm_small; cap_tml = ntm_large;
     lsd_tiles_cap = ltiles; seg_tiles_cap = stiles;
     KGB_CHECK(cudaMemset(d_lstat, 0, ltiles * 256 * 8));
     return 0;
@@ -1206,12 +1425,14 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 
 void FwdEngine::set_caps(FwdArgs &a) const {
     a.orand64 = d_orand64;
-    for (int q = 0; q < 2; q++) { a.lkey[q] = d_lkey[q]; a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
+    for (int q = 0; q < 2; q++) { a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
+    a.segbits = d_segbits;
     a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg;
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.warp_path = (u32)cfg.warp_path;
-    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_tms = cap_tms; a.cap_tml = cap_tml;
+    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_segt = cap_segt; a.cap_tms = cap_tms;
+    a.cap_tml = cap_tml;
 }
 
 int FwdEngine::plan(const u32 *n, const u32 *r, int count, bool want_sa) {
@@ -1390,7 +1611,8 @@ static int set_tile_attrs(int tile) {
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
     }
-    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
     g_attr_done[idx] = true;
     return 0;
 }
@@ -1489,7 +1711,9 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
         if (!((slots >> slot) & 1)) continue;
         L.tag(K_LSD_PASS, m_tag);
         if (L.prof) L.prof->pass = slot;
-        if ((e = L.go(k_lsd_pass, L.grid_lsd, TPB, lsd_smem(), a, slot))) return e;
+        if ((e = a.B > 1 ? L.go(k_lsd_pass<true>, L.grid_lsd, TPB, lsd_smem(), a, slot)
+                         : L.go(k_lsd_pass<false>, L.grid_lsd, TPB, lsd_smem(), a, slot)))
+            return e;
     }
     if (L.prof) L.prof->pass = -1;
     L.tag(K_SEG_COUNT, m_tag);
@@ -1588,6 +1812,10 @@ int FwdEngine::run_plain(cudaStream_t s) {
                 KGB_CHECK(enq_tile(L, a, prefix, false));
                 KGB_CHECK(enq_tile(L, a, prefix, true));
             }
+            if (!prefix && cnt_e(L_P0 + rp)) {
+                L.tag(K_GROUP, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
+                KGB_CHECK(L.go(k_group_thread, grid_msd, TPB, 0, a));
+            }
         }
         L.tag(K_CTL, 0);
         KGB_CHECK(L.go(k_ctl_round_end, 1, 1, 0, a));
@@ -1640,19 +1868,6 @@ static int add_while(cudaGraph_t g, Deps &deps, cudaGraphConditionalHandle h, cu
     return 0;
 }
 
-static int add_if(cudaGraph_t g, Deps &deps, cudaGraphConditionalHandle h, cudaGraph_t *body) {
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeIf;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node;
-    KGB_CHECK(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &cp));
-    *body = cp.conditional.phGraph_out[0];
-    deps.assign(1, node);
-    return 0;
-}
-
 // A tile-path round (prefix or rank) into graph g after deps; hmsd closes its bucket-pass loop.
 static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L, const FwdArgs &a, bool prefix,
                           cudaGraphConditionalHandle hmsd) {
@@ -1679,7 +1894,8 @@ static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L
     return capture_into(s, g, deps, [&]() -> cudaError_t {
         cudaError_t e;
         if ((e = enq_tile(L, a, prefix, false))) return e;
-        return enq_tile(L, a, prefix, true);
+        if ((e = enq_tile(L, a, prefix, true))) return e;
+        return prefix ? cudaSuccess : L.go(k_group_thread, L.grid_msd, TPB, 0, a);
     });
 }
 

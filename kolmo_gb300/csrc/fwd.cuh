@@ -29,6 +29,7 @@ enum : u32 {
     L_K0, L_K1,  // bucket-pass work lists (ping-pong across passes)
     L_KS,        // small buckets produced by the bucket passes, keys attached
     L_R0, L_R1,  // suffixes resolved in a round (their ranks are copied to the other rank buffer next round)
+    L_P0, L_P1,  // tiny groups (2..GTINY elements) of the rank rounds, one list per round parity
     NLISTS
 };
 
@@ -119,7 +120,7 @@ class FwdEngine {
     void set_caps(FwdArgs &a) const;
     bool lsd_enabled() const;
     u32 call_seq = 0;
-    u64 cap_segs = 0, cap_segl = 0, cap_tms = 0, cap_tml = 0;
+    u64 cap_segs = 0, cap_segl = 0, cap_segt = 0, cap_tms = 0, cap_tml = 0;
 
     // capacities
     u64 Ncap = 0;
@@ -144,10 +145,9 @@ class FwdEngine {
     u32 *d_hist = nullptr, *d_cursor = nullptr, *d_bhead = nullptr, *d_orand = nullptr;
     u64 *d_orand64 = nullptr;
     // LSD path
-    u64 *d_lkey[2] = {nullptr, nullptr};
     u32 *d_lval[2] = {nullptr, nullptr}, *d_lhi[2] = {nullptr, nullptr};
     u64 *d_lstat = nullptr;
-    u32 *d_lhist = nullptr, *d_ltile = nullptr, *d_segagg = nullptr;
+    u32 *d_lhist = nullptr, *d_ltile = nullptr, *d_segagg = nullptr, *d_segbits = nullptr;
     u64 lsd_tiles_cap = 0, seg_tiles_cap = 0;
     u8 *d_dest = nullptr;
     Ctl *d_ctl = nullptr;

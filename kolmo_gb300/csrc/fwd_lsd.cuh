@@ -1,23 +1,23 @@
 // Round 0 of the forward sort as one LSD radix sort: every suffix of the batch is sorted by (block, zero-padded
 // 8-byte prefix) with one pass per varying key byte (single-pass scatter with decoupled look-back), then a
-// segmentation turns the sorted keys into ranks, finished suffixes and the rank rounds' groups (the small-group list
-// for the tile kernels, the large-group list for the bucket passes). Included by fwd.cu inside namespace kgb, after
-// the kernels it shares (FwdArgs, resolve, tile-map writers).
+// segmentation turns the sorted order into ranks, finished suffixes and the rank rounds' groups (the small-group list
+// for the tile kernels, the large-group list for the bucket passes). The passes move only suffix ids (and block
+// indexes when the batch has several blocks): a pass reads its digit, one text byte, from the text, which stays in L2
+// while the ids stream through. Included by fwd.cu inside namespace kgb, after the kernels it shares (FwdArgs,
+// resolve, tile-map writers).
 #pragma once
 // (included inside namespace kgb)
 
-constexpr int LSD_IPT = 12, LSD_TILE = TPB * LSD_IPT;  // elements per sort tile
+constexpr int LSD_IPT = 16, LSD_TILE = TPB * LSD_IPT;  // elements per sort tile
 constexpr int NSLOT = 12;                              // digit slots: key bytes 0..7, then block-index bytes 0..3
 constexpr int SEG_IPT = 16, SEG_TILE = TPB * SEG_IPT;  // positions per segmentation tile (SEG_IPT <= 32)
 // look-back words: epoch (32 bits: call sequence, digit slot) | flag (2 bits) | value (30 bits); a word of another
 // epoch (an earlier slot or call) counts as not yet published
 constexpr u64 ST_AGG = 1ull << 30, ST_PRE = 2ull << 30, ST_VAL = (1ull << 30) - 1;
 constexpr u64 ST_EPOCH = 0xFFFFFFFF00000000ull;
+constexpr int LB_WIN = 8;  // look-back window (predecessor words read per step)
 
-__device__ __forceinline__ u32 slot_digit(u64 k, u32 hi, int slot) {
-    return slot < 8 ? (u32)(k >> (8 * slot)) & 0xFFu : (hi >> (8 * (slot - 8))) & 0xFFu;
-}
-__device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte s varies in this round
+__device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte s varies
     const u64 vl = c->vary_lo ^ c->and_lo;
     const u32 vh = c->vary_hi ^ c->and_hi;
     u32 m = 0;
@@ -27,9 +27,24 @@ __device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte 
     for (int s = 0; s < 4; s++) m |= ((vh >> (8 * s)) & 0xFF) ? 1u << (8 + s) : 0u;
     return m;
 }
-__device__ __forceinline__ bool lsd_has_hi(const FwdArgs &a) { return a.ctl->round == 0 && a.B > 1; }
+__device__ __forceinline__ bool lsd_has_hi(const FwdArgs &a) { return a.B > 1; }
 
-// Round start (256 threads): clear the digit histograms, the key OR/AND and the tile counters.
+// Digit `slot` of suffix id of block b: slots 0..7 are the bytes of its zero-padded 8-byte prefix, least significant
+// (text byte id + 7) first; slots 8..11 are the bytes of the block index.
+__device__ __forceinline__ u32 lsd_digit(const u8 *__restrict__ T, u32 id, u32 b, u64 end, int slot) {
+    if (slot >= 8) return (b >> (8 * (slot - 8))) & 0xFFu;
+    const u32 d = 7 - slot;
+    return (u64)id + d < end ? (u32)__ldg(T + id + d) : 0u;
+}
+// The zero-padded 8-byte prefix of suffix id (block ending at end) as a big-endian word.
+__device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u32 id, u64 end) {
+    u64 k = load_be64(T, id);
+    const u64 rem = end - id;
+    if (rem < 8) k &= ~0ull << (8 * (8 - rem));
+    return k;
+}
+
+// Start (256 threads): clear the digit histograms, the key OR/AND, the tile counters and the resolved count.
 __global__ void k_lsd_begin(FwdArgs a) {
     Ctl *c = a.ctl;
     for (int i = threadIdx.x; i < NSLOT * 256; i += blockDim.x) a.lhist[i] = 0;
@@ -56,11 +71,11 @@ __device__ __forceinline__ void orand_flush(Ctl *c, u64 ol, u64 al, u32 oh, u32 
     }
 }
 
-// Round 0 keys: the zero-padded 8-byte prefix of every suffix (block index in `hi` when the batch has several
-// blocks), in the dense order of the batch.
+// Suffix ids in the dense order of the batch (block index beside them when the batch has several blocks), and the
+// OR / AND of all keys, which tell the passes which key bytes vary.
 __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
     Ctl *c = a.ctl;
-    const bool hi = a.B > 1;
+    const bool hi = lsd_has_hi(a);
     const u64 stride = (u64)gridDim.x * blockDim.x;
     u64 ol = 0, al = ~0ull;
     u32 oh = 0, ah = ~0u;
@@ -71,13 +86,10 @@ __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
         for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < bi.n; j += stride) {
             const u32 id = bi.off + (u32)j;
-            u64 k = load_be64(a.T, id);
-            const u64 rem = end - id;
-            if (rem < 8) k &= ~0ull << (8 * (8 - rem));
+            const u64 k = lsd_key(a.T, id, end);
             const u64 x = (u64)bi.soff + j;
-            a.lkey[0][x] = k;
-            a.lval[0][x] = id;
-            if (hi) a.lhi[0][x] = b;
+            __stcs(a.lval[0] + x, id);
+            if (hi) __stcs(a.lhi[0] + x, b);
             ol |= k; al &= k; oh |= b; ah &= b;
         }
     }
@@ -95,13 +107,17 @@ __global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
     const int slot = __ffs(act) - 1;
     const bool hi = lsd_has_hi(a);
     const u32 m = c->m;
+    const u64 end0 = blk_end(a, 0);
     hs[threadIdx.x] = 0;
     __syncthreads();
     const u32 lane = lane_id();
     for (u32 x0 = blockIdx.x * blockDim.x; x0 < m; x0 += gridDim.x * blockDim.x) {
         const u32 x = x0 + threadIdx.x;
         u32 d = 0x100;
-        if (x < m) d = slot_digit(a.lkey[0][x], hi ? a.lhi[0][x] : 0u, slot);
+        if (x < m) {
+            const u32 b = hi ? a.lhi[0][x] : 0u;
+            d = lsd_digit(a.T, a.lval[0][x], b, hi ? blk_end(a, b) : end0, slot);
+        }
         const u32 peers = __match_any_sync(0xffffffffu, d);
         if (d < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&hs[d], __popc(peers));
     }
@@ -110,11 +126,11 @@ __global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
 }
 
 struct LsdSmem {
-    u64 key[LSD_TILE];
     u32 val[LSD_TILE];
     u32 hi[LSD_TILE];
+    u8 dg[LSD_TILE];
+    u8 nd[LSD_TILE];
     u16 wcnt[TPB / 32][256];
-    u32 dstart[256];
     u64 gbase[256];
     u32 dbase[256];
     u32 nh[256];
@@ -122,10 +138,11 @@ struct LsdSmem {
     u32 tile;
 };
 
-// One LSD pass over digit `slot` (skipped when that key byte is the same in every key): rank the tile's keys by
+// One LSD pass over digit `slot` (skipped when that key byte is the same in every key): rank the tile's suffixes by
 // digit, publish the tile's digit counts, look back over earlier tiles for the global offsets (bounded spin), stage
 // the tile in shared memory in digit order and write it out in runs; meanwhile count the next varying digit.
-__global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
+template <bool HI>
+__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
     const Ctl *c = a.ctl;
@@ -134,10 +151,10 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     const u32 par = __popc(act & ((1u << slot) - 1)) & 1;
     const u32 nxt_mask = act & ~((2u << slot) - 1);
     const int nslot = nxt_mask ? __ffs(nxt_mask) - 1 : -1;
-    const bool hi = lsd_has_hi(a);
     const u32 m = c->m;
     const u32 ntiles = (m + LSD_TILE - 1) / LSD_TILE;
     const u64 epoch = (u64)((c->seq << 4) | (u32)slot) << 32;
+    const u64 end0 = blk_end(a, 0);
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
     // digit bases of the pass: exclusive scan of the slot's histogram
@@ -152,25 +169,31 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     if (tile >= ntiles) return;
     const u32 base = tile * LSD_TILE;
     const u32 cnt = min((u32)LSD_TILE, m - base);
-    const u64 *kin = a.lkey[par];
     const u32 *vin = a.lval[par], *hin = a.lhi[par];
-    u64 k[LSD_IPT];
-    u32 v[LSD_IPT], hh[LSD_IPT], dg[LSD_IPT], rk[LSD_IPT];
+    // rk[j]: rank in the warp's digit bucket (bits 0..11) | digit, 0x100 past the end (bits 12..20) | next pass's
+    // digit (bits 21..28)
+    u32 v[LSD_IPT], hh[LSD_IPT], rk[LSD_IPT];
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
         const bool ok = x < cnt;
-        k[j] = ok ? kin[base + x] : 0ull;
-        v[j] = ok ? vin[base + x] : 0u;
-        hh[j] = ok && hi ? hin[base + x] : 0u;
-        dg[j] = ok ? slot_digit(k[j], hh[j], slot) : 0x100u;
+        v[j] = ok ? __ldcs(vin + base + x) : 0u;
+        hh[j] = ok && HI ? __ldcs(hin + base + x) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
-        const u32 d = dg[j];
+        const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
+        const u64 end = HI ? blk_end(a, hh[j]) : end0;
+        const u32 d = x < cnt ? lsd_digit(a.T, v[j], hh[j], end, slot) : 0x100u;
+        const u32 nd = x < cnt && nslot >= 0 ? lsd_digit(a.T, v[j], hh[j], end, nslot) : 0u;
+        rk[j] = (d << 12) | (nd << 21);
+    }
+#pragma unroll
+    for (int j = 0; j < LSD_IPT; j++) {
+        const u32 d = (rk[j] >> 12) & 0x1FFu;
         const u32 peers = __match_any_sync(0xffffffffu, d);
         const u32 before = d < 256 ? S.wcnt[warp][d] : 0u;
-        rk[j] = before + __popc(peers & lanemask_lt());
+        rk[j] |= before + __popc(peers & lanemask_lt());
         __syncwarp();
         if (d < 256 && (__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
         __syncwarp();
@@ -183,8 +206,7 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     u64 *st = a.lstat + (u64)tile * 256 + tid;
     if (tile == 0) atomicExch((unsigned long long *)st, epoch | ST_PRE | tot);
     else atomicExch((unsigned long long *)st, epoch | ST_AGG | tot);
-    u32 dstart = block_excl_sum<TPB>(tot, S.ws, nullptr);
-    S.dstart[tid] = dstart;
+    const u32 dstart = block_excl_sum<TPB>(tot, S.ws, nullptr);
     {
         u32 run = dstart;
 #pragma unroll
@@ -192,21 +214,35 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     }
     u64 excl = 0;
     if (tile > 0) {
+        // windowed look-back: read LB_WIN predecessors' words at once, add aggregates in order up to the first
+        // inclusive prefix; a word not yet published ends the window and the walk resumes there
         long j = (long)tile - 1;
         u32 spins = 0;
-        while (j >= 0) {
-            const u64 w = *(volatile u64 *)(a.lstat + (u64)j * 256 + tid);
-            if ((w & ST_EPOCH) != epoch || !(w & (ST_AGG | ST_PRE))) {
+        while (true) {
+            u64 w[LB_WIN];
+#pragma unroll
+            for (int q = 0; q < LB_WIN; q++)
+                w[q] = j - q >= 0 ? *(volatile u64 *)(a.lstat + (u64)(j - q) * 256 + tid) : 0ull;
+            int used = 0;
+            bool done = false;
+#pragma unroll
+            for (int q = 0; q < LB_WIN; q++) {
+                if (done || used < q) continue;  // stopped earlier in the window
+                const u64 x = w[q];
+                if ((x & ST_EPOCH) != epoch || !(x & (ST_AGG | ST_PRE))) continue;
+                excl += x & ST_VAL;
+                used = q + 1;
+                if (x & ST_PRE) done = true;
+            }
+            if (done) break;
+            j -= used;
+            if (used == 0) {
                 if (++spins > a.spin_limit) {  // a predecessor never published: report and stop waiting
                     atomicOr(&a.ctl->err, 256u);
                     break;
                 }
                 __nanosleep(32);
-                continue;
             }
-            excl += w & ST_VAL;
-            if (w & ST_PRE) break;
-            j--;
         }
         atomicExch((unsigned long long *)st, epoch | ST_PRE | (excl + tot));
     }
@@ -215,28 +251,26 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     // stage in digit order
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
-        if (dg[j] < 256) {
-            const u32 p = S.wcnt[warp][dg[j]] + rk[j];
-            S.key[p] = k[j];
+        const u32 d = (rk[j] >> 12) & 0x1FFu;
+        if (d < 256) {
+            const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFu);
             S.val[p] = v[j];
-            S.hi[p] = hh[j];
+            if (HI) S.hi[p] = hh[j];
+            S.dg[p] = (u8)d;
+            S.nd[p] = (u8)(rk[j] >> 21);
         }
     }
     __syncthreads();
-    u64 *kout = a.lkey[par ^ 1];
     u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1];
     for (u32 i = tid; i < LSD_TILE; i += TPB) {
         u32 d2 = 0x100;
         if (i < cnt) {
-            const u64 kk = S.key[i];
-            const u32 h2 = S.hi[i];
-            const u64 dst = S.gbase[slot_digit(kk, h2, slot)] + i;
+            const u64 dst = S.gbase[S.dg[i]] + i;
             if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
-                kout[dst] = kk;
-                vout[dst] = S.val[i];
-                if (hi) hout[dst] = h2;
+                __stcs(vout + dst, S.val[i]);
+                if (HI) __stcs(hout + dst, S.hi[i]);
             }
-            if (nslot >= 0) d2 = slot_digit(kk, h2, nslot);
+            if (nslot >= 0) d2 = S.nd[i];
         }
         if (nslot >= 0) {
             const u32 peers = __match_any_sync(0xffffffffu, d2);
@@ -253,13 +287,12 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
 // Positions are handled in tiles of SEG_TILE; warp w of a tile owns the SEG_IPT * 32 consecutive positions starting at
 // tile base + w * 32 * SEG_IPT and visits them lane-striped (position = chunk base + j * 32 + lane), so every load is
 // coalesced. Group starts are kept as a bitmask (bit p of the mask: a group starts at position p), written by the
-// count kernel into the free half of the key ping-pong; the emit kernels read only the bits.
+// count kernel (which compares neighbouring prefixes read from the text); the emit kernels read only the bits.
 __device__ __forceinline__ u32 lsd_final_par(const Ctl *c) { return __popc(active_slots(c)) & 1; }
 
 struct SegBufs {
-    const u64 *key;
     const u32 *val, *hi;
-    u32 *bits;          // start bitmask (free key buffer)
+    u32 *bits;          // start bitmask
     u32 *gbase, *gidx;  // per group start: list slot base, list index | GRP_LARGE (free value / block buffers)
     bool has_hi;
     u32 m;
@@ -268,15 +301,15 @@ __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
     const Ctl *c = a.ctl;
     const u32 par = lsd_final_par(c);
     SegBufs v;
-    v.key = a.lkey[par]; v.val = a.lval[par]; v.hi = a.lhi[par];
-    v.bits = reinterpret_cast<u32 *>(a.lkey[par ^ 1]);
+    v.val = a.lval[par]; v.hi = a.lhi[par];
+    v.bits = a.segbits;
     v.gbase = a.lval[par ^ 1];
     v.gidx = a.lhi[par ^ 1];
     v.has_hi = lsd_has_hi(a);
     v.m = c->m;
     return v;
 }
-constexpr u32 GRP_LARGE = 0x80000000u;
+constexpr u32 GRP_LARGE = 0x80000000u, GRP_TINY = 0x40000000u;
 constexpr u32 SEG_WORDS = SEG_IPT;  // mask words per warp chunk
 
 // Per tile: start bits and the tile's last group start (position 0 always starts a group).
@@ -285,6 +318,7 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     const SegBufs v = seg_bufs(a);
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 lane = lane_id(), warp = warp_id();
+    const u64 end0 = blk_end(a, 0);
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
         u32 last = 0;
@@ -292,11 +326,14 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
         for (int j = 0; j < SEG_IPT; j++) {
             const u32 p = cb + j * 32 + lane;
             const bool ok = p < v.m;
-            u64 k = ok ? v.key[p] : 0ull;
             u32 h = ok && v.has_hi ? v.hi[p] : 0u;
+            u64 k = ok ? lsd_key(a.T, v.val[p], v.has_hi ? blk_end(a, h) : end0) : 0ull;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1);
             u32 hp = __shfl_up_sync(0xffffffffu, h, 1);
-            if (lane == 0 && ok && p > 0) { kp = v.key[p - 1]; hp = v.has_hi ? v.hi[p - 1] : 0u; }
+            if (lane == 0 && ok && p > 0) {
+                hp = v.has_hi ? v.hi[p - 1] : 0u;
+                kp = lsd_key(a.T, v.val[p - 1], v.has_hi ? blk_end(a, hp) : end0);
+            }
             const bool st = ok && (p == 0 || k != kp || h != hp);
             const u32 b = __ballot_sync(0xffffffffu, st);
             if (lane == 0 && cb + j * 32 < v.m) v.bits[(cb >> 5) + j] = b;
@@ -396,25 +433,27 @@ __device__ __forceinline__ u64 block_excl_sum64(u64 v, u64 *ws, u64 *total) {
     return before + inc - v;
 }
 
-// Emit, part 1 (group ends): groups of one resolve; every other group takes its slots in the next small-group list
-// (<= SMAX) or large-group list, writes its descriptor and tile-map entries, and records its slot base and index at
-// its first position for part 2. Slots are allocated once per tile (a count pass, a block scan, one atomic per list).
+// Emit, part 1 (group ends): groups of one resolve; every other group takes its slots in the next tiny-group list
+// (<= GTINY), small-group list (<= SMAX) or large-group list, writes its descriptor (and tile-map entries), and records
+// its slot base and index at its first position for part 2. Slots are allocated once per tile (a count pass, a block
+// scan, one atomic per list).
 __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     __shared__ u32 wl[TPB / 32];
-    __shared__ u64 ws[2][TPB / 32];
-    __shared__ u64 base[3];
+    __shared__ u64 ws[3][TPB / 32];
+    __shared__ u64 base[4];
     Ctl *c = a.ctl;
     const SegBufs v = seg_bufs(a);
     const u32 rpar = c->rpar, round = c->round;
-    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)];
+    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
     const ListView res = a.lists[L_R0 + rpar];
     u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 TS = a.smax;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const SegChunk ch = seg_chunk(a, v, t, wl);
-        // count: singles | small groups << 16 | small elements << 32 ; large groups | large elements << 32
-        u64 cs = 0, cl = 0;
+        // count: singles | small groups << 16 | small elements << 32 ; large groups | large elements << 32 ;
+        // tiny groups | tiny elements << 32
+        u64 cs = 0, cl = 0, ct = 0;
         {
             u32 carry = ch.carry0;
             for (int j = 0; j < SEG_IPT; j++) {
@@ -423,14 +462,17 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
                 if (!ok || !en) continue;
                 const u32 len = p - gf + 1;
                 if (len == 1) cs += 1;
+                else if (len <= GTINY) ct += 1ull | ((u64)len << 32);
                 else if (len <= TS) cs += (1ull << 16) | ((u64)len << 32);
                 else cl += 1ull | ((u64)len << 32);
             }
         }
-        u64 ts, tl;
+        u64 ts, tl, tt;
         u64 xs = block_excl_sum64(cs, ws[0], &ts);
         u64 xl = block_excl_sum64(cl, ws[1], &tl);
+        u64 xt = block_excl_sum64(ct, ws[2], &tt);
         if (threadIdx.x == 0) {
+            base[3] = (u32)tt ? atomicAdd(&c->cnt[L_P0 + (rpar ^ 1)], (tt << 32) | (tt >> 32)) : 0ull;
             base[0] = (ts & 0xFFFF) ? atomicAdd(&c->cnt[L_R0 + rpar], ts & 0xFFFF) : 0ull;
             base[1] = (ts >> 16) & 0xFFFF ? atomicAdd(&c->cnt[L_S0 + (rpar ^ 1)], (((ts >> 16) & 0xFFFF) << 32) | (ts >> 32)) : 0ull;
             base[2] = (u32)tl ? atomicAdd(&c->cnt[L_L0 + (rpar ^ 1)], (tl << 32) | (tl >> 32)) : 0ull;
@@ -439,6 +481,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
         u32 r1 = (u32)base[0] + (u32)(xs & 0xFFFF);
         u32 sidx = (u32)(base[1] >> 32) + (u32)((xs >> 16) & 0xFFFF), se = (u32)base[1] + (u32)(xs >> 32);
         u32 lidx = (u32)(base[2] >> 32) + (u32)xl, le = (u32)base[2] + (u32)(xl >> 32);
+        u32 tidx = (u32)(base[3] >> 32) + (u32)xt, te = (u32)base[3] + (u32)(xt >> 32);
         u32 carry = ch.carry0;
         for (int j = 0; j < SEG_IPT; j++) {
             u32 p, gf; bool ok, st, en;
@@ -453,7 +496,15 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
             }
             Seg g;
             g.len = len; g.head = head; g.bd = b;
-            if (len <= TS) {
+            if (len <= GTINY) {
+                g.start = te;
+                KGB_GUARD(tidx < a.cap_segt && (u64)te + len <= a.cap_n, &c->err, E_SEG) {
+                    tl_.seg[tidx] = g;
+                    v.gbase[gf] = te;
+                    v.gidx[gf] = tidx | GRP_TINY;
+                }
+                tidx++; te += len;
+            } else if (len <= TS) {
                 g.start = se;
                 KGB_GUARD(sidx < a.cap_segs && (u64)se + len <= a.cap_n, &c->err, E_SEG) {
                     sl.seg[sidx] = g;
@@ -484,7 +535,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
     Ctl *c = a.ctl;
     const SegBufs v = seg_bufs(a);
     const u32 rpar = c->rpar;
-    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)];
+    const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
     u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -506,6 +557,8 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
                     if (slot % TSM == 0) {
                         KGB_GUARD(slot / TSM < a.cap_tml, &c->err, E_TMAP) ll.tmap[slot / TSM] = gi & ~GRP_LARGE;
                     }
+                } else if (gi & GRP_TINY) {
+                    tl_.eid[slot] = id;
                 } else {
                     sl.eid[slot] = id;
                 }
