@@ -1562,7 +1562,7 @@ static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const
     return a;
 }
 
-static size_t lsd_smem() { return sizeof(LsdSmem); }
+static size_t lsd_smem(bool hi) { return hi ? sizeof(LsdSmem<true>) : sizeof(LsdSmem<false>); }
 template <bool PREFIX, int TILE>
 static int tile_smem() { return (int)sizeof(TileSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
 template <bool PREFIX, int TILE>
@@ -1611,8 +1611,8 @@ static int set_tile_attrs(int tile) {
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
     }
-    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
-    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem(false)));
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem(true)));
     g_attr_done[idx] = true;
     return 0;
 }
@@ -1703,7 +1703,7 @@ static cudaError_t enq_lsd_keys(Launcher &L, const FwdArgs &a) {
     L.tag(K_LSD_KEY0, 0);
     if ((e = L.go(k_lsd_key0, L.grid_msd, TPB, 0, a))) return e;
     L.tag(K_LSD_HIST, 0);
-    return L.go(k_lsd_hist0, L.grid_msd, TPB, 0, a);
+    return L.go(k_lsd_hist0, 1, 256, 0, a);
 }
 static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u32 m_tag) {
     cudaError_t e;
@@ -1711,8 +1711,8 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
         if (!((slots >> slot) & 1)) continue;
         L.tag(K_LSD_PASS, m_tag);
         if (L.prof) L.prof->pass = slot;
-        if ((e = a.B > 1 ? L.go(k_lsd_pass<true>, L.grid_lsd, TPB, lsd_smem(), a, slot)
-                         : L.go(k_lsd_pass<false>, L.grid_lsd, TPB, lsd_smem(), a, slot)))
+        if ((e = a.B > 1 ? L.go(k_lsd_pass<true>, L.grid_lsd, TPB, lsd_smem(true), a, slot)
+                         : L.go(k_lsd_pass<false>, L.grid_lsd, TPB, lsd_smem(false), a, slot)))
             return e;
     }
     if (L.prof) L.prof->pass = -1;

@@ -44,134 +44,133 @@ __device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u32 id, u64 end
     return k;
 }
 
-// Start (256 threads): clear the digit histograms, the key OR/AND, the tile counters and the resolved count.
+// Start (256 threads): clear the text byte histogram, the tile counters and the resolved count.
 __global__ void k_lsd_begin(FwdArgs a) {
     Ctl *c = a.ctl;
     for (int i = threadIdx.x; i < NSLOT * 256; i += blockDim.x) a.lhist[i] = 0;
     if (threadIdx.x < NSLOT) a.ltile[threadIdx.x] = 0;
-    if (threadIdx.x == 0) {
-        c->vary_lo = 0; c->and_lo = ~0ull; c->vary_hi = 0; c->and_hi = ~0u;
-        c->cnt[L_R0 + c->rpar] = 0;
-    }
-}
-
-__device__ __forceinline__ void orand_flush(Ctl *c, u64 ol, u64 al, u32 oh, u32 ah) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        ol |= __shfl_xor_sync(0xffffffffu, ol, o);
-        al &= __shfl_xor_sync(0xffffffffu, al, o);
-        oh |= __shfl_xor_sync(0xffffffffu, oh, o);
-        ah &= __shfl_xor_sync(0xffffffffu, ah, o);
-    }
-    if (lane_id() == 0) {
-        if (ol) atomicOr(&c->vary_lo, ol);
-        if (al != ~0ull) atomicAnd(&c->and_lo, al);
-        if (oh) atomicOr(&c->vary_hi, oh);
-        if (ah != ~0u) atomicAnd(&c->and_hi, ah);
-    }
+    if (threadIdx.x == 0) c->cnt[L_R0 + c->rpar] = 0;
 }
 
 // Suffix ids in the dense order of the batch (block index beside them when the batch has several blocks), and the
-// OR / AND of all keys, which tell the passes which key bytes vary.
+// byte histogram of the whole text (row 0 of the histogram table), from which every pass's digit counts follow.
 __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
-    Ctl *c = a.ctl;
+    __shared__ u32 hs[256];
     const bool hi = lsd_has_hi(a);
     const u64 stride = (u64)gridDim.x * blockDim.x;
-    u64 ol = 0, al = ~0ull;
-    u32 oh = 0, ah = ~0u;
+    hs[threadIdx.x] = 0;
+    __syncthreads();
     for (u32 b = 0; b < a.B; b++) {
         const BlockInfo bi = a.blk[b];
-        const u64 end = (u64)bi.off + bi.n;
         // row 0 of the L column (the sentinel rotation) holds the block's last byte
         if (blockIdx.x == 0 && threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
         for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < bi.n; j += stride) {
             const u32 id = bi.off + (u32)j;
-            const u64 k = lsd_key(a.T, id, end);
             const u64 x = (u64)bi.soff + j;
             __stcs(a.lval[0] + x, id);
             if (hi) __stcs(a.lhi[0] + x, b);
-            ol |= k; al &= k; oh |= b; ah &= b;
+            atomicAdd(&hs[__ldg(a.T + id)], 1u);
         }
     }
-    if (!hi) { oh = 0; ah = 0; }
-    orand_flush(c, ol, al, oh, ah);
-    if (blockIdx.x == 0 && threadIdx.x == 0) c->m = a.B ? a.blk[a.B - 1].soff + a.blk[a.B - 1].n : 0;
+    __syncthreads();
+    if (hs[threadIdx.x]) atomicAdd(&a.lhist[threadIdx.x], hs[threadIdx.x]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->m = a.B ? a.blk[a.B - 1].soff + a.blk[a.B - 1].n : 0;
 }
 
-// Histogram of the lowest varying digit (the first pass); later passes build their successor's histogram.
-__global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
-    __shared__ u32 hs[256];
-    const Ctl *c = a.ctl;
-    const u32 act = active_slots(c);
-    if (!act) return;
-    const int slot = __ffs(act) - 1;
-    const bool hi = lsd_has_hi(a);
-    const u32 m = c->m;
-    const u64 end0 = blk_end(a, 0);
-    hs[threadIdx.x] = 0;
+// Digit counts of every pass (one CTA of 256 threads, thread = digit value). Suffix i of a block of n bytes has key
+// byte d = T[i + d] when i + d < n, else 0, so the counts of key byte d are the block's byte counts minus those of
+// its first min(d, n) bytes, plus min(d, n) zeros; block-index digits count each block's n. A slot whose counts sit
+// in one digit is constant: the vary words mark the others, which the passes run.
+__global__ void k_lsd_hist0(FwdArgs a) {
+    __shared__ u32 pre[8][256];  // pre[d][x]: bytes x among the first d bytes of every block (d = 1..7)
+    __shared__ u32 zeros[8];
+    __shared__ u32 hib[4][256];
+    __shared__ u32 flag[NSLOT];
+    const u32 x = threadIdx.x;
+    for (int d = 0; d < 8; d++) pre[d][x] = 0;
+    for (int q = 0; q < 4; q++) hib[q][x] = 0;
+    if (x < 8) zeros[x] = 0;
+    if (x < NSLOT) flag[x] = 0;
     __syncthreads();
-    const u32 lane = lane_id();
-    for (u32 x0 = blockIdx.x * blockDim.x; x0 < m; x0 += gridDim.x * blockDim.x) {
-        const u32 x = x0 + threadIdx.x;
-        u32 d = 0x100;
-        if (x < m) {
-            const u32 b = hi ? a.lhi[0][x] : 0u;
-            d = lsd_digit(a.T, a.lval[0][x], b, hi ? blk_end(a, b) : end0, slot);
+    for (u32 b = x; b < a.B; b += blockDim.x) {
+        const BlockInfo bi = a.blk[b];
+        for (u32 d = 1; d < 8; d++) {
+            if (d <= bi.n) atomicAdd(&pre[d][a.T[(u64)bi.off + d - 1]], 1u);
+            atomicAdd(&zeros[d], d < bi.n ? d : bi.n);  // min(d, n) zero digits per block
         }
-        const u32 peers = __match_any_sync(0xffffffffu, d);
-        if (d < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&hs[d], __popc(peers));
+        if (a.B > 1)
+            for (int q = 0; q < 4; q++) atomicAdd(&hib[q][(b >> (8 * q)) & 0xFF], bi.n);
     }
     __syncthreads();
-    if (hs[threadIdx.x]) atomicAdd(&a.lhist[slot * 256 + threadIdx.x], hs[threadIdx.x]);
+    // pre[d] holds the bytes at offset d - 1 only: accumulate to the first d bytes
+    for (int d = 2; d < 8; d++) pre[d][x] += pre[d - 1][x];
+    const u32 m = a.ctl->m;
+    const u32 h0 = a.lhist[x];  // byte counts of the whole text
+    for (int slot = 0; slot < 8; slot++) {
+        const u32 d = 7 - slot;
+        const u32 v = d ? h0 - pre[d][x] + (x == 0 ? zeros[d] : 0u) : h0;
+        a.lhist[slot * 256 + x] = v;
+        if (v != 0 && v != m) flag[slot] = 1;  // at least two digits occur
+    }
+    if (a.B > 1)
+        for (int q = 0; q < 4; q++) {
+            const u32 v = hib[q][x];
+            a.lhist[(8 + q) * 256 + x] = v;
+            if (v != 0 && v != m) flag[8 + q] = 1;
+        }
+    __syncthreads();
+    if (x == 0) {
+        Ctl *c = a.ctl;
+        u64 vl = 0;
+        u32 vh = 0;
+        for (int q = 0; q < 8; q++) if (flag[q]) vl |= 0xFFull << (8 * q);
+        for (int q = 0; q < 4; q++) if (flag[8 + q]) vh |= 0xFFu << (8 * q);
+        c->vary_lo = vl; c->and_lo = 0; c->vary_hi = vh; c->and_hi = 0;
+    }
 }
 
+template <bool HI>
 struct LsdSmem {
     u32 val[LSD_TILE];
-    u32 hi[LSD_TILE];
+    u32 hi[HI ? LSD_TILE : 1];
     u8 dg[LSD_TILE];
-    u8 nd[LSD_TILE];
     u16 wcnt[TPB / 32][256];
-    u64 gbase[256];
+    u32 gbase[256];
     u32 dbase[256];
-    u32 nh[256];
     u32 ws[TPB / 32 + 1];
     u32 tile;
 };
 
 // One LSD pass over digit `slot` (skipped when that key byte is the same in every key): rank the tile's suffixes by
 // digit, publish the tile's digit counts, look back over earlier tiles for the global offsets (bounded spin), stage
-// the tile in shared memory in digit order and write it out in runs; meanwhile count the next varying digit.
+// the tile in shared memory in digit order and write it out in runs.
 template <bool HI>
-__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
+__global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
+    LsdSmem<HI> &S = *reinterpret_cast<LsdSmem<HI> *>(smem_raw);
     const Ctl *c = a.ctl;
     const u32 act = active_slots(c);
     if (!((act >> slot) & 1)) return;
     const u32 par = __popc(act & ((1u << slot) - 1)) & 1;
-    const u32 nxt_mask = act & ~((2u << slot) - 1);
-    const int nslot = nxt_mask ? __ffs(nxt_mask) - 1 : -1;
     const u32 m = c->m;
     const u32 ntiles = (m + LSD_TILE - 1) / LSD_TILE;
     const u64 epoch = (u64)((c->seq << 4) | (u32)slot) << 32;
     const u64 end0 = blk_end(a, 0);
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
-    // digit bases of the pass: exclusive scan of the slot's histogram
+    // digit bases of the pass: exclusive scan of the slot's counts
     {
         const u32 hcount = a.lhist[slot * 256 + tid];
         S.dbase[tid] = block_excl_sum<TPB>(hcount, S.ws, nullptr);
     }
     for (int i = tid; i < (TPB / 32) * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
-    S.nh[tid] = 0;
     __syncthreads();
     const u32 tile = S.tile;
     if (tile >= ntiles) return;
     const u32 base = tile * LSD_TILE;
     const u32 cnt = min((u32)LSD_TILE, m - base);
     const u32 *vin = a.lval[par], *hin = a.lhi[par];
-    // rk[j]: rank in the warp's digit bucket (bits 0..11) | digit, 0x100 past the end (bits 12..20) | next pass's
-    // digit (bits 21..28)
+    // rk[j]: rank in the warp's digit bucket (bits 0..15) | digit, 0x100 past the end (bits 16..24)
     u32 v[LSD_IPT], hh[LSD_IPT], rk[LSD_IPT];
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
@@ -184,13 +183,11 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
         const u64 end = HI ? blk_end(a, hh[j]) : end0;
-        const u32 d = x < cnt ? lsd_digit(a.T, v[j], hh[j], end, slot) : 0x100u;
-        const u32 nd = x < cnt && nslot >= 0 ? lsd_digit(a.T, v[j], hh[j], end, nslot) : 0u;
-        rk[j] = (d << 12) | (nd << 21);
+        rk[j] = (x < cnt ? lsd_digit(a.T, v[j], hh[j], end, slot) : 0x100u) << 16;
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
-        const u32 d = (rk[j] >> 12) & 0x1FFu;
+        const u32 d = rk[j] >> 16;
         const u32 peers = __match_any_sync(0xffffffffu, d);
         const u32 before = d < 256 ? S.wcnt[warp][d] : 0u;
         rk[j] |= before + __popc(peers & lanemask_lt());
@@ -212,7 +209,19 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 #pragma unroll
         for (int w = 0; w < TPB / 32; w++) { const u32 cc = S.wcnt[w][tid]; S.wcnt[w][tid] = (u16)run; run += cc; }
     }
-    u64 excl = 0;
+    __syncthreads();
+    // stage in digit order (tile-local offsets only: the items leave registers before the look-back)
+#pragma unroll
+    for (int j = 0; j < LSD_IPT; j++) {
+        const u32 d = rk[j] >> 16;
+        if (d < 256) {
+            const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFFu);
+            S.val[p] = v[j];
+            if (HI) S.hi[p] = hh[j];
+            S.dg[p] = (u8)d;
+        }
+    }
+    u32 excl = 0;
     if (tile > 0) {
         // windowed look-back: read LB_WIN predecessors' words at once, add aggregates in order up to the first
         // inclusive prefix; a word not yet published ends the window and the walk resumes there
@@ -230,7 +239,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
                 if (done || used < q) continue;  // stopped earlier in the window
                 const u64 x = w[q];
                 if ((x & ST_EPOCH) != epoch || !(x & (ST_AGG | ST_PRE))) continue;
-                excl += x & ST_VAL;
+                excl += (u32)(x & ST_VAL);
                 used = q + 1;
                 if (x & ST_PRE) done = true;
             }
@@ -244,42 +253,17 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
                 __nanosleep(32);
             }
         }
-        atomicExch((unsigned long long *)st, epoch | ST_PRE | (excl + tot));
+        atomicExch((unsigned long long *)st, epoch | ST_PRE | (u64)(excl + tot));
     }
-    S.gbase[tid] = (u64)S.dbase[tid] + excl - dstart;
-    __syncthreads();
-    // stage in digit order
-#pragma unroll
-    for (int j = 0; j < LSD_IPT; j++) {
-        const u32 d = (rk[j] >> 12) & 0x1FFu;
-        if (d < 256) {
-            const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFu);
-            S.val[p] = v[j];
-            if (HI) S.hi[p] = hh[j];
-            S.dg[p] = (u8)d;
-            S.nd[p] = (u8)(rk[j] >> 21);
-        }
-    }
+    S.gbase[tid] = S.dbase[tid] + excl - dstart;
     __syncthreads();
     u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1];
-    for (u32 i = tid; i < LSD_TILE; i += TPB) {
-        u32 d2 = 0x100;
-        if (i < cnt) {
-            const u64 dst = S.gbase[S.dg[i]] + i;
-            if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
-                __stcs(vout + dst, S.val[i]);
-                if (HI) __stcs(hout + dst, S.hi[i]);
-            }
-            if (nslot >= 0) d2 = S.nd[i];
+    for (u32 i = tid; i < cnt; i += TPB) {
+        const u32 dst = S.gbase[S.dg[i]] + i;
+        if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
+            __stcs(vout + dst, S.val[i]);
+            if (HI) __stcs(hout + dst, S.hi[i]);
         }
-        if (nslot >= 0) {
-            const u32 peers = __match_any_sync(0xffffffffu, d2);
-            if (d2 < 256 && (__ffs(peers) - 1) == (int)lane) atomicAdd(&S.nh[d2], __popc(peers));
-        }
-    }
-    if (nslot >= 0) {
-        __syncthreads();
-        if (S.nh[tid]) atomicAdd(&a.lhist[nslot * 256 + tid], S.nh[tid]);
     }
 }
 
