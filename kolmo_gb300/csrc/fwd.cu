@@ -39,6 +39,7 @@ constexpr int IPM = TSM / TPB;
 constexpr u32 DEPTH_PREFIX = 8, DEPTH_RANK = 4;
 constexpr u32 WARP_GROUP = 32;  // groups up to this long are handled by one warp (k_tile_warp)
 constexpr u32 GTINY = 8;        // groups up to this long leave the rank rounds' tile lists for one thread each
+constexpr u32 GMED = 256;       // groups up to this long (and longer than GTINY) are sorted by one warp each
 // Seg.bd flag of small groups: the group came from the previous round's small-group list and passed that round
 // unsplit, so both rank buffers already hold its head (set only on groups whose input was a small-group list: a group
 // cut out of a larger one by the bucket passes has its parent's head in the other buffer).
@@ -69,7 +70,7 @@ struct FwdArgs {
     u32 *lhist, *ltile, *segagg;
     u32 spin_limit;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
-    u64 cap_n, cap_segs, cap_segl, cap_segt, cap_tms, cap_tml;
+    u64 cap_n, cap_segs, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
 };
 
 // device error bits
@@ -137,7 +138,7 @@ struct TileSmem {
     u32 ws2[TPB / 32 + 1];
     u64 red[4][TPB / 32];
     u32 bases[4];
-    u32 pbases[2];
+    u32 pbases[4];
 };
 
 __device__ __forceinline__ void write_tmap_small(const FwdArgs &a, u32 *tmap, u32 ts, u32 start, u32 len, u32 sidx) {
@@ -392,8 +393,9 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             }
         }
         __syncthreads();
-        // survivors and runs per destination: tiny runs (<= GTINY) to the tiny list, longer ones to the small list
-        u32 ns = 0, ng = 0, np = 0, ngp = 0;
+        // survivors and runs per destination: tiny runs (<= GTINY) to the tiny list, medium runs (<= GMED) to the
+        // medium list, longer ones to the small list
+        u32 ns = 0, ng = 0, np = 0, ngp = 0, nm = 0, ngm = 0;
         {
             u32 gf = carry;
 #pragma unroll
@@ -402,14 +404,19 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 if (x >= cnt) break;
                 if (st[j]) gf = x;
                 if (st[j] && en[j]) continue;
-                if ((u32)S.klo[gf] <= GTINY) { np++; ngp += st[j]; } else { ns++; ng += st[j]; }
+                const u32 rl = (u32)S.klo[gf];
+                if (rl <= GTINY) { np++; ngp += st[j]; }
+                else if (rl <= GMED) { nm++; ngm += st[j]; }
+                else { ns++; ng += st[j]; }
             }
         }
-        u32 tot_pack = 0, tot_packp = 0;
+        u32 tot_pack = 0, tot_packp = 0, tot_packm = 0;
         const u32 pre = block_excl_sum<TPB>(ns | (ng << 16), S.ws, &tot_pack);
         const u32 prep = block_excl_sum<TPB>(np | (ngp << 16), S.ws, &tot_packp);
+        const u32 prem = block_excl_sum<TPB>(nm | (ngm << 16), S.ws, &tot_packm);
         const u32 tot_s = tot_pack & 0xFFFFu, tot_g = tot_pack >> 16;
         const u32 tot_p = tot_packp & 0xFFFFu, tot_gp = tot_packp >> 16;
+        const u32 tot_m = tot_packm & 0xFFFFu, tot_gm = tot_packm >> 16;
         if (tid == 0) {
             atomicAdd(&a.ctl->tile_elems[0], (u64)cnt);
             if (tot_s) {
@@ -422,13 +429,19 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 S.pbases[0] = (u32)o;
                 S.pbases[1] = (u32)(o >> 32);
             }
-            S.bases[2] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)(cnt - tot_s - tot_p));
+            if (tot_m) {
+                const u64 o = atomicAdd(&a.ctl->cnt[L_M0 + (rpar ^ 1)], ((u64)tot_gm << 32) | tot_m);
+                S.pbases[2] = (u32)o;
+                S.pbases[3] = (u32)(o >> 32);
+            }
+            S.bases[2] = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)(cnt - tot_s - tot_p - tot_m));
         }
         __syncthreads();
-        const ListView outp = a.lists[L_P0 + (rpar ^ 1)];
+        const ListView outp = a.lists[L_P0 + (rpar ^ 1)], outm = a.lists[L_M0 + (rpar ^ 1)];
         const u32 ebase = S.bases[0], sbase = S.bases[1], rbase = S.bases[2];
-        const u32 pebase = S.pbases[0], psbase = S.pbases[1];
+        const u32 pebase = S.pbases[0], psbase = S.pbases[1], mebase = S.pbases[2], msbase = S.pbases[3];
         u32 es = pre & 0xFFFFu, gs = pre >> 16, ep = prep & 0xFFFFu, gp = prep >> 16;
+        u32 em = prem & 0xFFFFu, gm = prem >> 16;
         u32 gfirst = carry;
 #pragma unroll
         for (int j = 0; j < IPT; j++) {
@@ -441,7 +454,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
             const bool unsplit = !(lh >> 31);
             if (st[j] && en[j]) {
                 // finished suffixes take the resolved slots in position order after the survivors before them
-                resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + (x - es - ep));
+                resolve(a, isa_nxt, id, (lh & 0x7FFFFFFFu) + (x - s0), seg_blk(bd), res, rbase + (x - es - ep - em));
                 continue;
             }
             const u32 head = (lh & 0x7FFFFFFFu) + (gfirst - s0);
@@ -461,6 +474,15 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                     KGB_GUARD(psbase + gp - 1 < a.cap_segt, &a.ctl->err, E_SEG) outp.seg[psbase + gp - 1] = g;
                 }
                 ep++;
+            } else if (len <= GMED) {
+                KGB_GUARD(mebase + em < a.cap_n, &a.ctl->err, E_LIST) outm.eid[mebase + em] = id;
+                if (st[j]) gm++;
+                if (en[j]) {
+                    Seg g;
+                    g.start = mebase + em + 1 - len; g.len = len; g.head = head; g.bd = sbd;
+                    KGB_GUARD(msbase + gm - 1 < a.cap_segm, &a.ctl->err, E_SEG) outm.seg[msbase + gm - 1] = g;
+                }
+                em++;
             } else {
                 KGB_GUARD(ebase + es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + es] = id;
                 if (st[j]) gs++;
@@ -508,7 +530,6 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
     const u32 rpar = ctl->rpar, h = ctl->h, round = ctl->round;
     const u32 lin = KEYED ? L_KS : L_S0 + rpar;
     const ListView in = a.lists[lin];
-    const ListView out = a.lists[L_S0 + (rpar ^ 1)];
     const ListView res = a.lists[L_R0 + rpar];
     const u64 c = ctl->cnt[lin];
     const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
@@ -677,8 +698,8 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
         u32 ebase = 0, sbase = 0, rbase = 0, pebase = 0, psbase = 0;
         if (lane == 0) {
             atomicAdd(&a.ctl->tile_elems[1], (u64)(X1 - X0));
-            if (ns) {
-                const u64 o = atomicAdd(&a.ctl->cnt[L_S0 + (rpar ^ 1)], ((u64)ng << 32) | ns);
+            if (ns) {  // runs of 9..WARP_GROUP go to the medium list
+                const u64 o = atomicAdd(&a.ctl->cnt[L_M0 + (rpar ^ 1)], ((u64)ng << 32) | ns);
                 ebase = (u32)o; sbase = (u32)(o >> 32);
             }
             if (np) {
@@ -692,7 +713,7 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
         rbase = __shfl_sync(0xffffffffu, rbase, 0);
         pebase = __shfl_sync(0xffffffffu, pebase, 0);
         psbase = __shfl_sync(0xffffffffu, psbase, 0);
-        const ListView outp = a.lists[L_P0 + (rpar ^ 1)];
+        const ListView outp = a.lists[L_P0 + (rpar ^ 1)], outm = a.lists[L_M0 + (rpar ^ 1)];
         // ---- emit
         u32 es = 0, gs = 0, ep = 0, gp = 0, rs = 0, carry = X0;  // running counts; carry: start of the open run
         for (u32 xb = X0; xb < X1; xb += 32) {
@@ -737,14 +758,12 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
                             KGB_GUARD(sidx < a.cap_segt, &a.ctl->err, E_SEG) outp.seg[sidx] = g;
                         }
                     } else {
-                        KGB_GUARD(ebase + my_es < a.cap_n, &a.ctl->err, E_LIST) out.eid[ebase + my_es] = id;
+                        KGB_GUARD(ebase + my_es < a.cap_n, &a.ctl->err, E_LIST) outm.eid[ebase + my_es] = id;
                         if (en) {
                             const u32 sidx = sbase + my_gs + (st ? 1u : 0u) - 1u;
-                            const u32 start = ebase + my_es + 1 - len;
                             Seg g;
-                            g.start = start; g.len = len; g.head = head; g.bd = sbd;
-                            KGB_GUARD(sidx < a.cap_segs, &a.ctl->err, E_SEG) out.seg[sidx] = g;
-                            write_tmap_small(a, out.tmap, TS, start, len, sidx);
+                            g.start = ebase + my_es + 1 - len; g.len = len; g.head = head; g.bd = sbd;
+                            KGB_GUARD(sidx < a.cap_segm, &a.ctl->err, E_SEG) outm.seg[sidx] = g;
                         }
                     }
                 }
@@ -871,6 +890,193 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
     }
 }
 #undef KGB_CS
+
+// ------------------------------------------------------------------------------------------------ medium groups
+// Rank rounds: one warp per group of GTINY+1..GMED suffixes. A flat pass first gathers every member's raw key
+// rank(i + h) into a scratch array in list order (all loads independent); the group's warp then loads ids and raw keys
+// with coalesced reads, corrects the keys of suffixes whose i + h lies past their block, sorts in its shared-memory
+// slice (counting for groups of up to 32, bitonic network otherwise), and walks the sorted runs twice: once for their
+// lengths and offsets in the next lists, once to emit ranks, finished suffixes and runs (tiny ones to the tiny list,
+// the others to the medium list).
+
+// Raw keys of the medium list: mkey[x] = ISA[eid[x] + h] (clamped into the rank buffer; corrected per block later).
+__global__ void __launch_bounds__(TPB) k_mkeys(FwdArgs a) {
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h;
+    const ListView in = a.lists[L_M0 + rpar];
+    const u32 nelem = min((u32)ctl->cnt[L_M0 + rpar], (u32)a.cap_n);
+    const u32 *isa_cur = a.isa[rpar];
+    u32 *mk = a.lval[0];
+    for (u32 x = blockIdx.x * TPB + threadIdx.x; x < nelem; x += gridDim.x * TPB) {
+        const u64 j = (u64)in.eid[x] + h;
+        mk[x] = j < a.cap_n ? __ldg(isa_cur + j) : 0u;
+    }
+}
+
+struct GWarpSmem {
+    u32 key[2][GMED];  // [1]: keys being sorted / sorted; [0]: run lengths and offsets after the sort
+    u32 val[2][GMED];
+};
+
+__global__ void __launch_bounds__(TPB) k_group_warp(FwdArgs a) {
+    __shared__ GWarpSmem SM[TPB / 32];
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar, h = ctl->h;
+    const ListView in = a.lists[L_M0 + rpar], outm = a.lists[L_M0 + (rpar ^ 1)], outp = a.lists[L_P0 + (rpar ^ 1)];
+    const ListView res = a.lists[L_R0 + rpar];
+    const u64 c = ctl->cnt[L_M0 + rpar];
+    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
+    if (nelem > a.cap_n || nseg > a.cap_segm) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
+        return;
+    }
+    const u32 *mk = a.lval[0];
+    u32 *isa_nxt = a.isa[rpar ^ 1];
+    const u32 lane = lane_id(), lt = lanemask_lt();
+    GWarpSmem &W = SM[warp_id()];
+    u32 *K = W.key[1], *V = W.val[1];
+    u16 *RL = reinterpret_cast<u16 *>(W.key[0]);  // run length at the run's first sorted position
+    u16 *RO = RL + GMED;                           // run's element offset within its destination
+    u16 *RG = reinterpret_cast<u16 *>(W.val[0]);   // run's segment offset within its destination
+    const u32 gw = blockIdx.x * (TPB / 32) + warp_id(), nw = gridDim.x * (TPB / 32);
+    for (u32 s = gw; s < nseg; s += nw) {
+        const Seg g = in.seg[s];
+        const u32 len = g.len;
+        if (len > GMED || len < 2 || (u64)g.start + len > nelem) {  // broken list invariant: report, skip
+            if (lane == 0) atomicOr(&a.ctl->err, E_SEG);
+            continue;
+        }
+        const u32 b = seg_blk(g.bd);
+        const u64 end = blk_end(a, b);
+        if (len <= 32) {
+            // ---- counting sort, one member per lane (position = keys below + equal keys before)
+            u32 id = 0, kx = 0xFFFFFFFFu;
+            if (lane < len) {
+                id = in.eid[g.start + lane];
+                const u32 d = (u32)(end - id);
+                kx = h < d ? mk[g.start + lane] + h : d - 1;
+            }
+            u32 below = 0;
+            for (u32 y = 0; y < len; y++) {
+                const u32 ky = __shfl_sync(0xffffffffu, kx, y);
+                below += ky < kx || (ky == kx && y < lane);
+            }
+            if (lane < len) { K[below] = kx; V[below] = id; }
+        } else {
+            // ---- bitonic sort of the group padded to a power of two (padding keys sort last)
+            const u32 p2 = 1u << (32 - __clz(len - 1));
+            for (u32 q = lane; q < p2; q += 32) {
+                u32 id = 0, kx = 0xFFFFFFFFu;
+                if (q < len) {
+                    id = in.eid[g.start + q];
+                    const u32 d = (u32)(end - id);
+                    kx = h < d ? mk[g.start + q] + h : d - 1;
+                }
+                K[q] = kx;
+                V[q] = id;
+            }
+            __syncwarp();
+            for (u32 k = 2; k <= p2; k <<= 1) {
+                for (u32 j = k >> 1; j > 0; j >>= 1) {
+                    for (u32 t = lane; t < p2 / 2; t += 32) {
+                        const u32 i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), l = i + j;
+                        const u32 ki = K[i], kl = K[l];
+                        if ((ki > kl) == ((i & k) == 0) && ki != kl) {
+                            const u32 vi = V[i];
+                            K[i] = kl; K[l] = ki;
+                            V[i] = V[l]; V[l] = vi;
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        __syncwarp();
+        const bool unsplit = K[0] == K[len - 1];
+        // ---- runs: lengths and offsets (per destination) at each run's first position
+        u32 carry = 0, off_p = 0, off_m = 0, g_p = 0, g_m = 0, n1 = 0;
+        for (u32 c0 = 0; c0 < len; c0 += 32) {
+            const u32 q = c0 + lane;
+            const bool valid = q < len;
+            bool st = false, en = false;
+            if (valid) {
+                const u32 kq = K[q];
+                st = q == 0 || kq != K[q - 1];
+                en = q + 1 == len || kq != K[q + 1];
+            }
+            const u32 gf = max(carry, warp_incl_max(valid && st ? q : 0u));
+            const u32 rl = valid && en ? q - gf + 1 : 0u;
+            const u32 pe = rl >= 2 && rl <= GTINY ? rl : 0u, me = rl > GTINY ? rl : 0u;
+            const u32 pei = warp_incl_sum(pe), mei = warp_incl_sum(me);
+            const u32 bp = __ballot_sync(0xffffffffu, pe != 0), bm = __ballot_sync(0xffffffffu, me != 0);
+            const u32 b1 = __ballot_sync(0xffffffffu, rl == 1);
+            if (rl >= 2) {
+                RL[gf] = (u16)rl;
+                RO[gf] = (u16)(pe ? off_p + pei - pe : off_m + mei - me);
+                RG[gf] = (u16)(pe ? g_p + __popc(bp & lt) : g_m + __popc(bm & lt));
+            }
+            off_p += __shfl_sync(0xffffffffu, pei, 31);
+            off_m += __shfl_sync(0xffffffffu, mei, 31);
+            g_p += __popc(bp);
+            g_m += __popc(bm);
+            n1 += __popc(b1);
+            carry = __shfl_sync(0xffffffffu, gf, 31);
+        }
+        u32 pb = 0, psb = 0, mb = 0, msb = 0, rb = 0;
+        if (lane == 0) {
+            if (off_p) { const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)g_p << 32) | off_p); pb = (u32)o; psb = (u32)(o >> 32); }
+            if (off_m) { const u64 o = atomicAdd(&a.ctl->cnt[L_M0 + (rpar ^ 1)], ((u64)g_m << 32) | off_m); mb = (u32)o; msb = (u32)(o >> 32); }
+            if (n1) rb = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)n1);
+        }
+        pb = __shfl_sync(0xffffffffu, pb, 0); psb = __shfl_sync(0xffffffffu, psb, 0);
+        mb = __shfl_sync(0xffffffffu, mb, 0); msb = __shfl_sync(0xffffffffu, msb, 0);
+        rb = __shfl_sync(0xffffffffu, rb, 0);
+        __syncwarp();
+        // ---- emit
+        const bool skip_rank = (g.bd & STABLE) && unsplit;
+        const u32 sbd = b | (unsplit ? STABLE : 0u);
+        carry = 0;
+        u32 r1 = 0;
+        for (u32 c0 = 0; c0 < len; c0 += 32) {
+            const u32 q = c0 + lane;
+            const bool valid = q < len;
+            bool st = false, en = false;
+            if (valid) {
+                const u32 kq = K[q];
+                st = q == 0 || kq != K[q - 1];
+                en = q + 1 == len || kq != K[q + 1];
+            }
+            const u32 gf = max(carry, warp_incl_max(valid && st ? q : 0u));
+            carry = __shfl_sync(0xffffffffu, gf, 31);
+            const bool single = valid && st && en;
+            const u32 b1 = __ballot_sync(0xffffffffu, single);
+            const u32 my1 = r1 + __popc(b1 & lt);
+            r1 += __popc(b1);
+            if (!valid) continue;
+            const u32 id = V[q];
+            if (single) {
+                resolve(a, isa_nxt, id, g.head + q, b, res, rb + my1);
+                continue;
+            }
+            const u32 head = g.head + gf;
+            if (!skip_rank) {
+                KGB_GUARD(id < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[id] = head;
+            }
+            const u32 rl = RL[gf], ro = RO[gf], rg = RG[gf];
+            const bool tiny = rl <= GTINY;
+            const ListView &o = tiny ? outp : outm;
+            const u32 eb = (tiny ? pb : mb) + ro;
+            KGB_GUARD(eb + (q - gf) < a.cap_n, &a.ctl->err, E_LIST) o.eid[eb + (q - gf)] = id;
+            if (en) {
+                Seg ng_;
+                ng_.start = eb; ng_.len = rl; ng_.head = head; ng_.bd = sbd;
+                const u32 si = (tiny ? psb : msb) + rg;
+                KGB_GUARD(si < (tiny ? a.cap_segt : a.cap_segm), &a.ctl->err, E_SEG) o.seg[si] = ng_;
+            }
+        }
+        __syncwarp();
+    }
+}
 
 // ------------------------------------------------------------------------------------------------ bucket passes
 // Work lists of large groups are tiled by TSM elements; every group is longer than TSM, so a tile meets at most
@@ -1264,10 +1470,12 @@ __global__ void k_ctl_msd_next(FwdArgs a) {
 __global__ void k_ctl_round_end(FwdArgs a) {
     Ctl *c = a.ctl;
     const u32 rp = c->rpar;
-    const u32 active = elems(c, L_S0 + (rp ^ 1)) + elems(c, L_L0 + (rp ^ 1)) + elems(c, L_P0 + (rp ^ 1));
+    const u32 active = elems(c, L_S0 + (rp ^ 1)) + elems(c, L_L0 + (rp ^ 1)) + elems(c, L_P0 + (rp ^ 1)) +
+                       elems(c, L_M0 + (rp ^ 1));
     c->cnt[L_S0 + rp] = 0;
     c->cnt[L_L0 + rp] = 0;
     c->cnt[L_P0 + rp] = 0;
+    c->cnt[L_M0 + rp] = 0;
     c->cnt[L_KS] = 0;
     c->cnt[L_K0] = 0;
     c->cnt[L_K1] = 0;
@@ -1343,6 +1551,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     const u32 smax = (u32)cfg.tile_cap / 2;
     const u64 nseg_small = n / 2 + bcap + 8;
     const u64 nseg_large = n / smax + bcap + 8;
+    const u64 nseg_med = n / (GTINY + 1) + bcap + 8;
     const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
     struct Item { void **p; size_t bytes; };
     std::vector<Item> items;
@@ -1360,9 +1569,9 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
         add((void **)&lists[l].eid, n * 4);
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
-        const bool tiny = l == L_P0 || l == L_P1;
-        if (tiny) {  // ids and segment descriptors only
-            add((void **)&lists[l].seg, nseg_small * sizeof(Seg));
+        const bool tiny = l == L_P0 || l == L_P1, med = l == L_M0 || l == L_M1;
+        if (tiny || med) {  // ids and segment descriptors only
+            add((void **)&lists[l].seg, (tiny ? nseg_small : nseg_med) * sizeof(Seg));
             continue;
         }
         if (l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
@@ -1417,7 +1626,8 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     Bcap = bcap;
     Icap = icap;
     sa_cap = want_sa;
-    cap_segs = nseg_small; cap_segl = nseg_large; cap_segt = nseg_small; cap_tms = ntm_small; cap_tml = ntm_large;
+    cap_segs = nseg_small; cap_segl = nseg_large; cap_segt = nseg_small; cap_segm = nseg_med; cap_tms = ntm_small;
+    cap_tml = ntm_large;
     lsd_tiles_cap = ltiles; seg_tiles_cap = stiles;
     KGB_CHECK(cudaMemset(d_lstat, 0, ltiles * 256 * 8));
     return 0;
@@ -1431,7 +1641,8 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.warp_path = (u32)cfg.warp_path;
-    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_segt = cap_segt; a.cap_tms = cap_tms;
+    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_segt = cap_segt; a.cap_segm = cap_segm;
+    a.cap_tms = cap_tms;
     a.cap_tml = cap_tml;
 }
 
@@ -1812,6 +2023,12 @@ int FwdEngine::run_plain(cudaStream_t s) {
                 KGB_CHECK(enq_tile(L, a, prefix, false));
                 KGB_CHECK(enq_tile(L, a, prefix, true));
             }
+            if (!prefix && cnt_e(L_M0 + rp)) {
+                L.tag(K_MKEYS, cnt_e(L_M0 + rp), cnt_s(L_M0 + rp));
+                KGB_CHECK(L.go(k_mkeys, grid_msd, TPB, 0, a));
+                L.tag(K_GROUP_WARP, cnt_e(L_M0 + rp), cnt_s(L_M0 + rp));
+                KGB_CHECK(L.go(k_group_warp, grid_scan, TPB, 0, a));
+            }
             if (!prefix && cnt_e(L_P0 + rp)) {
                 L.tag(K_GROUP, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
                 KGB_CHECK(L.go(k_group_thread, grid_msd, TPB, 0, a));
@@ -1895,7 +2112,10 @@ static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L
         cudaError_t e;
         if ((e = enq_tile(L, a, prefix, false))) return e;
         if ((e = enq_tile(L, a, prefix, true))) return e;
-        return prefix ? cudaSuccess : L.go(k_group_thread, L.grid_msd, TPB, 0, a);
+        if (prefix) return cudaSuccess;
+        if ((e = L.go(k_mkeys, L.grid_msd, TPB, 0, a))) return e;
+        if ((e = L.go(k_group_warp, L.grid_scan, TPB, 0, a))) return e;
+        return L.go(k_group_thread, L.grid_msd, TPB, 0, a);
     });
 }
 

@@ -30,6 +30,7 @@ enum : u32 {
     L_KS,        // small buckets produced by the bucket passes, keys attached
     L_R0, L_R1,  // suffixes resolved in a round (their ranks are copied to the other rank buffer next round)
     L_P0, L_P1,  // tiny groups (2..GTINY elements) of the rank rounds, one list per round parity
+    L_M0, L_M1,  // medium groups (GTINY+1..GMED elements) of the rank rounds, one list per round parity
     NLISTS
 };
 
@@ -120,7 +121,7 @@ class FwdEngine {
     void set_caps(FwdArgs &a) const;
     bool lsd_enabled() const;
     u32 call_seq = 0;
-    u64 cap_segs = 0, cap_segl = 0, cap_segt = 0, cap_tms = 0, cap_tml = 0;
+    u64 cap_segs = 0, cap_segl = 0, cap_segt = 0, cap_segm = 0, cap_tms = 0, cap_tml = 0;
 
     // capacities
     u64 Ncap = 0;

@@ -293,7 +293,7 @@ __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
     v.m = c->m;
     return v;
 }
-constexpr u32 GRP_LARGE = 0x80000000u, GRP_TINY = 0x40000000u;
+constexpr u32 GRP_LARGE = 0x80000000u, GRP_TINY = 0x40000000u, GRP_MED = 0x20000000u;
 constexpr u32 SEG_WORDS = SEG_IPT;  // mask words per warp chunk
 
 // Per tile: start bits and the tile's last group start (position 0 always starts a group).
@@ -418,17 +418,18 @@ __device__ __forceinline__ u64 block_excl_sum64(u64 v, u64 *ws, u64 *total) {
 }
 
 // Emit, part 1 (group ends): groups of one resolve; every other group takes its slots in the next tiny-group list
-// (<= GTINY), small-group list (<= SMAX) or large-group list, writes its descriptor (and tile-map entries), and records
-// its slot base and index at its first position for part 2. Slots are allocated once per tile (a count pass, a block
-// scan, one atomic per list).
+// (<= GTINY), medium-group list (<= GMED), small-group list (<= SMAX) or large-group list, writes its descriptor (and
+// tile-map entries), and records its slot base and index at its first position for part 2. Slots are allocated once
+// per tile (a count pass, a block scan, one atomic per list).
 __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     __shared__ u32 wl[TPB / 32];
-    __shared__ u64 ws[3][TPB / 32];
-    __shared__ u64 base[4];
+    __shared__ u64 ws[4][TPB / 32];
+    __shared__ u64 base[5];
     Ctl *c = a.ctl;
     const SegBufs v = seg_bufs(a);
     const u32 rpar = c->rpar, round = c->round;
     const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
+    const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
     const ListView res = a.lists[L_R0 + rpar];
     u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
@@ -436,8 +437,8 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const SegChunk ch = seg_chunk(a, v, t, wl);
         // count: singles | small groups << 16 | small elements << 32 ; large groups | large elements << 32 ;
-        // tiny groups | tiny elements << 32
-        u64 cs = 0, cl = 0, ct = 0;
+        // tiny groups | tiny elements << 32 ; medium groups | medium elements << 32
+        u64 cs = 0, cl = 0, ct = 0, cm = 0;
         {
             u32 carry = ch.carry0;
             for (int j = 0; j < SEG_IPT; j++) {
@@ -447,6 +448,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
                 const u32 len = p - gf + 1;
                 if (len == 1) cs += 1;
                 else if (len <= GTINY) ct += 1ull | ((u64)len << 32);
+                else if (len <= GMED) cm += 1ull | ((u64)len << 32);
                 else if (len <= TS) cs += (1ull << 16) | ((u64)len << 32);
                 else cl += 1ull | ((u64)len << 32);
             }
@@ -455,7 +457,10 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
         u64 xs = block_excl_sum64(cs, ws[0], &ts);
         u64 xl = block_excl_sum64(cl, ws[1], &tl);
         u64 xt = block_excl_sum64(ct, ws[2], &tt);
+        u64 tm;
+        u64 xm = block_excl_sum64(cm, ws[3], &tm);
         if (threadIdx.x == 0) {
+            base[4] = (u32)tm ? atomicAdd(&c->cnt[L_M0 + (rpar ^ 1)], (tm << 32) | (tm >> 32)) : 0ull;
             base[3] = (u32)tt ? atomicAdd(&c->cnt[L_P0 + (rpar ^ 1)], (tt << 32) | (tt >> 32)) : 0ull;
             base[0] = (ts & 0xFFFF) ? atomicAdd(&c->cnt[L_R0 + rpar], ts & 0xFFFF) : 0ull;
             base[1] = (ts >> 16) & 0xFFFF ? atomicAdd(&c->cnt[L_S0 + (rpar ^ 1)], (((ts >> 16) & 0xFFFF) << 32) | (ts >> 32)) : 0ull;
@@ -466,6 +471,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
         u32 sidx = (u32)(base[1] >> 32) + (u32)((xs >> 16) & 0xFFFF), se = (u32)base[1] + (u32)(xs >> 32);
         u32 lidx = (u32)(base[2] >> 32) + (u32)xl, le = (u32)base[2] + (u32)(xl >> 32);
         u32 tidx = (u32)(base[3] >> 32) + (u32)xt, te = (u32)base[3] + (u32)(xt >> 32);
+        u32 midx = (u32)(base[4] >> 32) + (u32)xm, me = (u32)base[4] + (u32)(xm >> 32);
         u32 carry = ch.carry0;
         for (int j = 0; j < SEG_IPT; j++) {
             u32 p, gf; bool ok, st, en;
@@ -488,6 +494,14 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
                     v.gidx[gf] = tidx | GRP_TINY;
                 }
                 tidx++; te += len;
+            } else if (len <= GMED) {
+                g.start = me;
+                KGB_GUARD(midx < a.cap_segm && (u64)me + len <= a.cap_n, &c->err, E_SEG) {
+                    ml_.seg[midx] = g;
+                    v.gbase[gf] = me;
+                    v.gidx[gf] = midx | GRP_MED;
+                }
+                midx++; me += len;
             } else if (len <= TS) {
                 g.start = se;
                 KGB_GUARD(sidx < a.cap_segs && (u64)se + len <= a.cap_n, &c->err, E_SEG) {
@@ -520,6 +534,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
     const SegBufs v = seg_bufs(a);
     const u32 rpar = c->rpar;
     const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
+    const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
     u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -543,6 +558,8 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
                     }
                 } else if (gi & GRP_TINY) {
                     tl_.eid[slot] = id;
+                } else if (gi & GRP_MED) {
+                    ml_.eid[slot] = id;
                 } else {
                     sl.eid[slot] = id;
                 }
