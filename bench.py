@@ -359,6 +359,152 @@ def run_ours(args, world, rank, local):
     return out
 
 
+def run_batch(args, world, rank, local):
+    """The mixed batch (256 blocks of 16 KiB-16 MiB, log-uniform; order-2 Markov, ACGT with 0.1% N, templated log
+    lines): one step = forward + inverse of every block. Timed three ways: the batched graph path (one engine call
+    per direction for the whole batch, device-resident buffers), the plain per-block path (one call per block,
+    host-driven rounds), and e2e through the batch C ABI (kgbwt_fwd_batch / kgbwt_inv_batch, host buffers). Each
+    rank takes a longest-first share of the blocks (weak scaling by blocks, no collective)."""
+    import torch
+
+    from kolmo_gb300 import codec, native
+    from kolmo_gb300 import workloads as W
+    from kolmo_gb300.host import codec18_rlog, n_samples
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    allb = W.mixed_batch()
+    mine = shard([int(t.size) for _, t in allb], rank, world)
+    texts = [allb[i][1] for i in mine]
+    offs, o = [], 0
+    for t in texts:
+        offs.append(o)
+        o += (t.size + 15) // 16 * 16
+    total = sum(int(t.size) for t in texts)
+    rs = [1 << codec18_rlog(int(t.size)) for t in texts]
+    iouts, k = [], 0
+    for t, r in zip(texts, rs):
+        iouts.append(k)
+        k += n_samples(int(t.size), r)
+    hbuf = np.zeros(o + 64, np.uint8)
+    for t, off in zip(texts, offs):
+        hbuf[off:off + t.size] = t
+    dT = torch.from_numpy(hbuf).to(dev)
+    dL = torch.zeros(o + len(texts) + 64, dtype=torch.uint8, device=dev)
+    dI = torch.zeros(k, dtype=torch.int32, device=dev)
+    dU = torch.zeros_like(dT)
+    dOut = torch.zeros_like(dT)
+    flush = torch.empty(256 * MIB, dtype=torch.uint8, device=dev)
+    s = torch.cuda.Stream(device=dev)
+    eng = codec.Engine()
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0)
+    fblocks = [(off, int(t.size), r, io) for t, off, r, io in zip(texts, offs, rs, iouts)]
+
+    def to_u(b_list, I):
+        with torch.cuda.stream(s):
+            for (off, n, r, io), bi in b_list:
+                p0 = int(I[io])
+                dU[off:off + p0].copy_(dL[off + bi:off + bi + p0])
+                dU[off + p0:off + n].copy_(dL[off + bi + p0 + 1:off + bi + n + 1])
+
+    def step_batched():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(s)
+        if eng.fwd(dT, dL, dI, fblocks, stream=s) or eng.wait()[0]:
+            raise RuntimeError(f"batched forward failed: {native.last_error()}")
+        I = dI.cpu().numpy()
+        to_u([(fb, b) for b, fb in enumerate(fblocks)], I)
+        iblocks = [(off, n, int(I[io])) for off, n, r, io in fblocks]
+        if eng.inv(dU, dOut, iblocks, stream=s) or eng.wait(len(iblocks))[0]:
+            raise RuntimeError(f"batched inverse failed: {native.last_error()}")
+        ev[1].record(s)
+        return ev
+
+    def step_plain():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(s)
+        for b, (off, n, r, io) in enumerate(fblocks):
+            # one block per call, laid out as a batch of one at the block's own offset
+            if eng.fwd(dT[off:], dL[off + b:], dI[io:], [(0, n, r, 0)], stream=s, plain=True) or eng.wait()[0]:
+                raise RuntimeError(f"plain forward failed: {native.last_error()}")
+            p0 = int(dI[io].item())
+            with torch.cuda.stream(s):
+                dU[off:off + p0].copy_(dL[off + b:off + b + p0])
+                dU[off + p0:off + n].copy_(dL[off + b + p0 + 1:off + b + n + 1])
+            if eng.inv(dU[off:], dOut[off:], [(0, n, p0)], stream=s, plain=True) or eng.wait(1)[0]:
+                raise RuntimeError(f"plain inverse failed: {native.last_error()}")
+        ev[1].record(s)
+        return ev
+
+    for _ in range(max(args.warmup, 1)):
+        step_batched()
+    s.synchronize()
+    for t, off in zip(texts, offs):
+        assert torch.equal(dOut[off:off + t.size].cpu(), torch.from_numpy(t)), "batched round trip failed"
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    tb = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(s):
+            flush.fill_(1)
+        ev = step_batched()
+        s.synchronize()
+        tb += ev[0].elapsed_time(ev[1])
+    clk = clocks.stop()
+    barrier(world)
+    tb = reduce_max(tb, world, dev)
+    value = world * args.steps * total / MIB / (tb / 1e3)
+    # the plain per-block path: one untimed pass, then one timed pass
+    dOut.zero_()
+    step_plain()
+    s.synchronize()
+    ev = step_plain()
+    s.synchronize()
+    tp = reduce_max(ev[0].elapsed_time(ev[1]), world, dev)
+    for t, off in zip(texts, offs):
+        assert torch.equal(dOut[off:off + t.size].cpu(), torch.from_numpy(t)), "plain round trip failed"
+    plain_v = world * total / MIB / (tp / 1e3)
+    ws = eng.workspace_bytes()
+    eng.close()  # the C ABI below sorts on the library's own engine: release this one's workspace first
+    del dT, dL, dI, dU, dOut, flush
+    torch.cuda.empty_cache()
+    # e2e: the batch C ABI with host buffers
+    jobs = [(t, r) for t, r in zip(texts, rs)]
+    rc, outs = codec.fwd_batch(jobs)
+    assert rc == 0 and all(o_[0] == 0 for o_ in outs)
+    ijobs = [(U, r, I) for (_, U, I), r in zip(outs, rs)]
+    barrier(world)
+    te = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rc, outs = codec.fwd_batch(jobs)
+        rc2, backs = codec.inv_batch([(U, r, I) for (_, U, I), r in zip(outs, rs)])
+        te += time.perf_counter() - t0
+        assert rc == 0 and rc2 == 0
+    for (rcb, back), t in zip(backs, texts):
+        assert rcb == 0 and np.array_equal(back, t), "C ABI batch round trip failed"
+    te = reduce_max(te, world, dev)
+    e2e_v = world * args.steps * total / MIB / te
+    out = {
+        "metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tb / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "batch256: 256 blocks, log-uniform 16 KiB-16 MiB (order-2 Markov, ACGT, log lines), "
+                               "forward + inverse BWT, one graph launch per direction",
+                   "blocks": len(texts), "bytes": total, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"blocks sharded longest-first over {world} rank(s)"},
+        "plain_per_block_MiB_per_s": round(plain_v, 2),
+        "batched_over_plain": round(value / plain_v, 2),
+        "e2e": {"value": round(e2e_v, 2), "unit": "MiB/s", "h2d_bytes_per_step": 2 * total,
+                "d2h_bytes_per_step": 2 * total + 4 * k, "path": "kgbwt_fwd_batch + kgbwt_inv_batch, host buffers"},
+        "workspace_bytes": ws,
+        "clocks": clk,
+    }
+    return out
+
+
 def run_e2e(T, r, steps, warmup, world, dev):
     import torch
 
@@ -439,7 +585,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="prose64", choices=["prose64"])
+    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch"])
     ap.add_argument("--block-mib", type=int, default=64, help="block size (the benchmark configuration is 64)")
     ap.add_argument("--tile-cap", type=int, default=0, help="engine tile capacity (4096 or 8192; 0 = default)")
     ap.add_argument("--tile-ctas", type=int, default=0)
@@ -462,7 +608,7 @@ def main():
     import torch
 
     dist_init(world, "nccl" if torch.cuda.is_available() else "gloo")
-    out = run_ours(args, world, rank, local)
+    out = run_batch(args, world, rank, local) if args.workload == "batch" else run_ours(args, world, rank, local)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

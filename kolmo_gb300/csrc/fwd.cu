@@ -70,7 +70,7 @@ struct FwdArgs {
     u32 *lhist, *ltile, *segagg;
     u32 spin_limit;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
-    u64 cap_n, cap_segs, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
+    u64 cap_n, cap_segs, cap_segk, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
 };
 
 // device error bits
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
     const ListView res = a.lists[L_R0 + rpar];
     const u64 c = ctl->cnt[lin];
     const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
-    if (nelem > a.cap_n || nseg > a.cap_segs) {
+    if (nelem > a.cap_n || nseg > (KEYED ? a.cap_segk : a.cap_segs)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
         return;
     }
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
     const ListView res = a.lists[L_R0 + rpar];
     const u64 c = ctl->cnt[lin];
     const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
-    if (nelem > a.cap_n || nseg > a.cap_segs) {
+    if (nelem > a.cap_n || nseg > (KEYED ? a.cap_segk : a.cap_segs)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
         return;
     }
@@ -1316,7 +1316,7 @@ __global__ void __launch_bounds__(TPB) k_msd_scan(FwdArgs a) {
             else { start = S.base_e[C_LN] + x_ln; sidx = S.base_s[C_LN] + ((x_sp >> 20) & 1023); o = a.lists[lln]; }
             Seg ng;
             ng.start = start; ng.len = cc; ng.head = head; ng.bd = bd;
-            KGB_GUARD(sidx < (cls == C_KS ? a.cap_segs : a.cap_segl) && (u64)start + cc <= a.cap_n, &a.ctl->err, E_SEG)
+            KGB_GUARD(sidx < (cls == C_KS ? a.cap_segk : a.cap_segl) && (u64)start + cc <= a.cap_n, &a.ctl->err, E_SEG)
             o.seg[sidx] = ng;
             a.cursor[hrow + tid] = start;
             if (cls == C_KS) {
@@ -1552,6 +1552,9 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     const u64 nseg_small = n / 2 + bcap + 8;
     const u64 nseg_large = n / smax + bcap + 8;
     const u64 nseg_med = n / (GTINY + 1) + bcap + 8;
+    // small-group lists hold groups longer than GMED (every producer sends shorter ones to the tiny and medium
+    // lists), besides one group per block in the tile path's round 0; the keyed list takes any bucket size
+    const u64 nseg_s = n / (GMED + 1) + bcap + 8;
     const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
     struct Item { void **p; size_t bytes; };
     std::vector<Item> items;
@@ -1576,7 +1579,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
         }
         if (l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
         if (!res) {
-            add((void **)&lists[l].seg, (small ? nseg_small : nseg_large) * sizeof(Seg));
+            add((void **)&lists[l].seg, (l == L_KS ? nseg_small : small ? nseg_s : nseg_large) * sizeof(Seg));
             add((void **)&lists[l].tmap, (small ? ntm_small : ntm_large) * 4);
             if (small) add((void **)&lists[l].tbig, ntm_small * 4);
         }
@@ -1626,7 +1629,8 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     Bcap = bcap;
     Icap = icap;
     sa_cap = want_sa;
-    cap_segs = nseg_small; cap_segl = nseg_large; cap_segt = nseg_small; cap_segm = nseg_med; cap_tms = ntm_small;
+    cap_segs = nseg_s; cap_segk = nseg_small; cap_segl = nseg_large; cap_segt = nseg_small; cap_segm = nseg_med;
+    cap_tms = ntm_small;
     cap_tml = ntm_large;
     lsd_tiles_cap = ltiles; seg_tiles_cap = stiles;
     KGB_CHECK(cudaMemset(d_lstat, 0, ltiles * 256 * 8));
@@ -1641,7 +1645,8 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.warp_path = (u32)cfg.warp_path;
-    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segl = cap_segl; a.cap_segt = cap_segt; a.cap_segm = cap_segm;
+    a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segk = cap_segk; a.cap_segl = cap_segl; a.cap_segt = cap_segt;
+    a.cap_segm = cap_segm;
     a.cap_tms = cap_tms;
     a.cap_tml = cap_tml;
 }

@@ -121,7 +121,7 @@ class FwdEngine {
     void set_caps(FwdArgs &a) const;
     bool lsd_enabled() const;
     u32 call_seq = 0;
-    u64 cap_segs = 0, cap_segl = 0, cap_segt = 0, cap_segm = 0, cap_tms = 0, cap_tml = 0;
+    u64 cap_segs = 0, cap_segk = 0, cap_segl = 0, cap_segt = 0, cap_segm = 0, cap_tms = 0, cap_tml = 0;
 
     // capacities
     u64 Ncap = 0;

@@ -8,8 +8,11 @@
 // psi is built by a stable counting sort of the L column by byte (psi[C[c] + k] = row of the k-th c in L).
 //
 // Parallel decode (the chain idea of libsais's split decoder, sais.c:11573-11703, re-designed for a GPU):
-//   * rows p0 and every multiple of MARK are marks; bit 31 of psi[x] flags "psi[x] is a mark" so a walk learns it
-//     reached the next mark from the load it needs anyway;
+//   * row p0 and about one row in MARK are marks; bit 31 of psi[x] flags "psi[x] is a mark" so a walk learns it
+//     reached the next mark from the load it needs anyway. The regular marks are the rows (m * hmul) mod 2^k for
+//     m = 1..n/MARK (2^k >= n, hmul odd near 2^k / golden ratio): a Weyl sequence, so the marks spread evenly over
+//     every arithmetic progression of rows. Rows every MARK apart would leave whole stretches of a periodic text
+//     unmarked (its rows interleave the periods), and one thread would walk each such stretch alone;
 //   * one chain per mark walks psi until the next mark (or row 0), writing its bytes into its own CAPC-byte
 //     buffer; a walk that reaches CAPC bytes closes its chain and continues as a new chain, so buffers never overflow
 //     and no row is walked twice;
@@ -57,7 +60,19 @@ struct InvArgs {
     u64 cap_n;  // bytes of the text buffers (checked build)
 };
 
-__device__ __forceinline__ u32 is_mark(u32 q, u32 p0) { return q != 0 && (q % MARK == 0 || q == p0); }
+// Chain id of a regular mark at row q (in 1..nreg when q is one).
+__device__ __forceinline__ u32 mark_id(u32 q, const InvBlock &B) { return (q * B.hinv) & B.hmask; }
+__device__ __forceinline__ u32 is_mark(u32 q, const InvBlock &B) {
+    if (q == 0) return 0;
+    const u32 m = mark_id(q, B);
+    return q == B.p0 || (m >= 1 && m <= B.nreg);
+}
+// Start row of chain id (0: p0; m >= 1: the m-th regular mark, or none (0) when that row is past n or is p0).
+__device__ __forceinline__ u32 chain_start(u32 id, const InvBlock &B) {
+    if (id == 0) return B.p0;
+    const u32 q = (id * B.hmul) & B.hmask;
+    return q > B.n || q == B.p0 ? 0u : q;
+}
 
 // Per-chunk byte histograms (a chunk is CHUNKT consecutive tiles of one block).
 __global__ void __launch_bounds__(ITPB) k_inv_chunkhist(InvArgs a) {
@@ -170,7 +185,7 @@ __global__ void __launch_bounds__(ITPB) k_inv_scatter(InvArgs a) {
                     const u32 u = start + x;
                     const u32 qr = u + (u >= B.p0);
                     const u32 dst = woff[warp][cs[j]] + rk[j];
-                    KGB_GUARD(dst >= 1 && dst <= B.n, &a.status[b], 0x100) psi[dst] = qr | (is_mark(qr, B.p0) << 31);
+                    KGB_GUARD(dst >= 1 && dst <= B.n, &a.status[b], 0x100) psi[dst] = qr | (is_mark(qr, B) << 31);
                 }
             }
             __syncthreads();
@@ -186,8 +201,8 @@ __device__ __forceinline__ u32 f_of(const u32 *Cs, u32 row) {  // largest c with
     return lo;
 }
 
-// Walk every chain of a work item (block, [c0, c1) start chains). Chain 0 starts at p0; chain m >= 1 at row m*MARK
-// (none when that row is p0). Chains that reach CAPC bytes continue under a new id taken from the block's counter.
+// Walk every chain of a work item (block, [c0, c1) start chains). Chain 0 starts at p0; chain m >= 1 at its mark
+// (none when that row is past n or is p0). Chains that reach CAPC bytes continue under a new id taken from the block's counter.
 __global__ void __launch_bounds__(ITPB) k_inv_walk(InvArgs a) {
     __shared__ u32 Cs[257];
     for (u32 w = blockIdx.x; w < a.nchunks; w += gridDim.x) {
@@ -206,8 +221,8 @@ __global__ void __launch_bounds__(ITPB) k_inv_walk(InvArgs a) {
             while (next < c1) {
                 const u32 id = next;
                 next += ITPB;
-                const u32 start = id == 0 ? B.p0 : id * MARK;
-                if (id != 0 && start == B.p0) continue;  // chain 0 covers the mark at p0
+                const u32 start = chain_start(id, B);
+                if (start == 0) continue;  // no such row, or chain 0 covers the mark at p0
                 row[k] = start; steps[k] = 0; acc[k] = 0; cid[k] = id; act[k] = true;
                 break;
             }
@@ -240,13 +255,13 @@ __global__ void __launch_bounds__(ITPB) k_inv_walk(InvArgs a) {
                     if (steps[k] & 3) reinterpret_cast<u32 *>(a.buf + g * CAPC)[steps[k] >> 2] = acc[k];
                     a.len[g] = steps[k];
                     if (stop) {
-                        a.succ[g] = nxt == 0 ? ENDC : B.chain_base + (nxt == B.p0 ? 0u : nxt / MARK);
+                        a.succ[g] = nxt == 0 ? ENDC : B.chain_base + (nxt == B.p0 ? 0u : mark_id(nxt, B));
                         act[k] = false;
                         while (next < c1) {
                             const u32 id = next;
                             next += ITPB;
-                            const u32 start = id == 0 ? B.p0 : id * MARK;
-                            if (id != 0 && start == B.p0) continue;
+                            const u32 start = chain_start(id, B);
+                            if (start == 0) continue;
                             row[k] = start; steps[k] = 0; acc[k] = 0; cid[k] = id; act[k] = true;
                             break;
                         }
@@ -377,6 +392,18 @@ int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
     return 0;
 }
 
+// Mark parameters of a block of B.n bytes: the smallest 2^k >= n, the Weyl multiplier and its inverse. Rows run
+// 0..n; when n = 2^k, row n maps to id 0 and is never a regular mark.
+static void mark_params(InvBlock &B) {
+    int k = 1;
+    while (k < 32 && (1ull << k) < B.n) k++;
+    B.hmask = (u32)((1ull << k) - 1);
+    B.hmul = (u32)(0x9E3779B97F4A7C15ull >> (64 - k)) | 1u;
+    u32 inv = B.hmul;  // Newton iteration for the inverse mod 2^32 (each step doubles the correct low bits)
+    for (int it = 0; it < 5; it++) inv *= 2u - B.hmul * inv;
+    B.hinv = inv;
+}
+
 static int plan_layout(const u32 *off, const u32 *n, const u32 *p0, int count, std::vector<InvBlock> &blk,
                        std::vector<u32> &cblk, std::vector<u32> &chunks, u64 &nchunk_all, u64 &nchains, u32 &maxchains) {
     blk.resize(count);
@@ -390,6 +417,7 @@ static int plan_layout(const u32 *off, const u32 *n, const u32 *p0, int count, s
         B.chunk_base = (u32)nchunk_all;
         B.nchunk = (n[b] + ITILE * CHUNKT - 1) / (ITILE * CHUNKT);
         B.nreg = n[b] / MARK;
+        mark_params(B);
         B.chain_base = (u32)nchains;
         B.chain_cap = B.nreg + 1 + n[b] / CAPC + 4;
         for (u32 t = 0; t < B.nchunk; t++) cblk.push_back((u32)b);
@@ -582,6 +610,7 @@ static int unbwt_noalloc(const u8 *dU, u8 *dT, u32 n, u32 p0, cudaStream_t s) {
     B.off = 0; B.n = n; B.p0 = p0;
     B.chunk_base = 0; B.nchunk = (n + ITILE * CHUNKT - 1) / (ITILE * CHUNKT);
     B.nreg = n / MARK; B.chain_base = 0; B.chain_cap = B.nreg + 1 + n / CAPC + 4;
+    mark_params(B);
     u32 cblk[NA_CHUNKS] = {0};
     u32 chunks[3 * NA_WALK];
     u32 nwalk = 0;

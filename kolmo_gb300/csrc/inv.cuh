@@ -13,8 +13,11 @@ struct InvBlock {
     u32 chunk_base;  // first 64 KiB chunk of the block (psi build)
     u32 nchunk;
     u32 chain_base;  // first chain record of the block
-    u32 nreg;        // regular marks (rows M, 2M, ..., nreg * M)
+    u32 nreg;        // regular marks: chain m in 1..nreg starts at row (m * hmul) & hmask when that row is <= n
     u32 chain_cap;   // chain records reserved for the block
+    u32 hmask;       // 2^k - 1 with 2^k >= n
+    u32 hmul;        // odd multiplier: the top k bits of 2^64 / golden ratio (rows of the marks are a Weyl sequence)
+    u32 hinv;        // hmul^-1 mod 2^32: row q is mark (q * hinv) & hmask
 };
 
 struct InvStats {

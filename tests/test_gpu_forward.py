@@ -139,3 +139,20 @@ def test_full_size_prose_round_trip_and_oracle():
     assert np.array_equal(I, oI) and np.array_equal(U, oU)
     rc, back = codec.unbwt_aux(U, r, I)
     assert rc == 0 and np.array_equal(back, T)
+
+
+def test_full_size_degenerate_blocks():
+    """The 128 MiB degenerate inputs (periodic with periods 1, 7 and 4096 and one random flip per MiB; Fibonacci
+    word): the GPU inverse restores the text from the GPU forward; for periodic-1 and Fibonacci the oracle's inverse
+    (an LF walk restated from the reference) also decodes the GPU's BWT and sampled indexes."""
+    n = 128 << 20
+    r = 1 << codec18_rlog(n)
+    for kind in ("periodic-1", "periodic-7", "periodic-4096", "fibonacci"):
+        T = W.degenerate(kind, n)
+        rc, U, I = codec.bwt_aux(T, r)
+        assert rc == 0, (kind, native.last_error())
+        rc, back = codec.unbwt_aux(U, r, I)
+        assert rc == 0 and np.array_equal(back, T), kind
+        if kind in ("periodic-1", "fibonacci"):
+            orc, oback = O.unbwt_aux(U, r, I)
+            assert orc == 0 and np.array_equal(oback, T), kind
