@@ -505,6 +505,115 @@ def run_batch(args, world, rank, local):
     return out
 
 
+def run_serve(args, world, rank, local):
+    """The serving workload: Poisson arrivals (rate --rate per second) of compress (30%, forward BWT) and decompress
+    (70%, inverse BWT) requests, lognormal sizes (median 256 KiB, sigma 1.5, capped at 128 MiB) from the three batch
+    sources, on the request server (--slots workers, 150 GB HBM budget, host buffers in and out). Reports p50/p99
+    latency (submission to completion) and MiB/s (request bytes over first arrival to last completion), next to the
+    serial per-request plain path on the same arrivals (each request's plain-path service time measured alone, then
+    a FIFO single server replayed over the arrival times). Each rank serves its own stream (weak scaling)."""
+    import threading
+
+    import torch
+
+    from kolmo_gb300 import codec, native
+    from kolmo_gb300 import workloads as W
+    from kolmo_gb300.host import codec18_rlog
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    count = args.requests
+    sizes, gaps, mix, src = W.requests(W.SEED_SERVE + rank, count, rate=args.rate)
+    reqs = []
+    for i in range(count):
+        n = max(int(sizes[i]), 2)
+        T = W.source_block(int(src[i]), n, W.SEED_SERVE * 7 + i)
+        r = 1 << codec18_rlog(n)
+        reqs.append(("fwd" if mix[i] < 300 else "inv", T, r))
+    # decompress payloads: the BWT of each decompress request (made before the timed region)
+    payload = []
+    for kind, T, r in reqs:
+        if kind == "inv":
+            rc, U, I = codec.bwt_aux(T, r)
+            assert rc == 0
+            payload.append((U, I))
+        else:
+            payload.append(None)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    total = sum(int(T.size) for _, T, _ in reqs)
+
+    def serve_once():
+        srv = codec.Server(slots=args.slots, hbm_budget=150 * 10**9)
+        handles = [None] * count
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, (kind, T, r) in enumerate(reqs):
+                d = t0 + arrivals[i] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                handles[i] = srv.submit_fwd(T, r) if kind == "fwd" else srv.submit_inv(payload[i][0], r, payload[i][1])
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        th.join()
+        lat = np.zeros(count)
+        for i, h in enumerate(handles):
+            st, rc, us = srv.wait(h[0], 600000)
+            if st != 1 or rc != 0:
+                raise RuntimeError(f"request {i} failed: {st} {rc} {native.last_error()}")
+            lat[i] = us / 1e3
+        t_end = time.perf_counter()
+        stats = srv.stats()
+        # results equal the drop-in calls (spot check every 8th request)
+        for i in range(0, count, 8):
+            kind, T, r = reqs[i]
+            if kind == "fwd":
+                rc, U, I = codec.bwt_aux(T, r)
+                assert np.array_equal(handles[i][1], U) and np.array_equal(handles[i][2], I)
+            else:
+                assert np.array_equal(handles[i][1], T)
+        srv.close()
+        return lat, t_end - t0, stats
+
+    for _ in range(max(args.warmup, 1) if args.warmup else 1):
+        serve_once()
+    barrier(world)
+    lat, wall, stats = serve_once()
+    value = total / MIB / wall
+    # serial per-request plain path: service times alone, then a FIFO single server over the same arrivals
+    svc = np.zeros(count)
+    for i, (kind, T, r) in enumerate(reqs):
+        t1 = time.perf_counter()
+        if kind == "fwd":
+            rc, outs = codec.fwd_batch([(T, r)], plain=True)
+        else:
+            rc, outs = codec.inv_batch([(payload[i][0], r, payload[i][1])], plain=True)
+        svc[i] = time.perf_counter() - t1
+        assert rc == 0
+    fin = 0.0
+    slat = np.zeros(count)
+    for i in range(count):
+        start = max(arrivals[i], fin)
+        fin = start + svc[i]
+        slat[i] = (fin - arrivals[i]) * 1e3
+    serial_v = total / MIB / fin
+    value = reduce_max(-value, world, dev) * -1.0 if world > 1 else value
+    return {
+        "metric": "serve_MiB_per_s", "value": round(world * value, 2), "unit": "MiB/s", "n_gpus": world,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": round(wall * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"serve: {count} Poisson requests at {args.rate}/s, 30% compress / 70% decompress, "
+                               "lognormal sizes (median 256 KiB, sigma 1.5, cap 128 MiB), batch sources",
+                   "slots": args.slots, "hbm_budget": 150 * 10**9, "bytes": total},
+        "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+        "serial_plain": {"value": round(serial_v, 2), "unit": "MiB/s",
+                         "p50_ms": round(float(np.percentile(slat, 50)), 3),
+                         "p99_ms": round(float(np.percentile(slat, 99)), 3)},
+        "server": {"batches": stats["batches"], "hbm_peak": stats["hbm_peak"]},
+    }
+
+
 def run_e2e(T, r, steps, warmup, world, dev):
     import torch
 
@@ -585,7 +694,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch"])
+    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch", "serve"])
+    ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests per second)")
+    ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
+    ap.add_argument("--slots", type=int, default=3, help="serve: server workers")
     ap.add_argument("--block-mib", type=int, default=64, help="block size (the benchmark configuration is 64)")
     ap.add_argument("--tile-cap", type=int, default=0, help="engine tile capacity (4096 or 8192; 0 = default)")
     ap.add_argument("--tile-ctas", type=int, default=0)
@@ -608,7 +720,12 @@ def main():
     import torch
 
     dist_init(world, "nccl" if torch.cuda.is_available() else "gloo")
-    out = run_batch(args, world, rank, local) if args.workload == "batch" else run_ours(args, world, rank, local)
+    if args.workload == "batch":
+        out = run_batch(args, world, rank, local)
+    elif args.workload == "serve":
+        out = run_serve(args, world, rank, local)
+    else:
+        out = run_ours(args, world, rank, local)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -140,6 +140,47 @@ const char *kgbwt_kernel_name(int32_t kernel);
  * device address; make that first call before any stream capture. */
 int32_t kgbwt_unbwt_noalloc(const uint8_t *dU, uint8_t *dT, int32_t n, int32_t p0, void *stream);
 
+/* ---- request server -----------------------------------------------------------------------------------------------
+ * No counterpart in the reference (its block workers call the sorter directly, src/core/blocks.c:181 and
+ * src/core/pool.c:74). Compress (forward) and decompress (inverse) requests on host buffers are queued and run by
+ * `slots` workers (1..16), each with its own engines and stream, so batches of different workers overlap on the GPU.
+ * Continuous batching: a worker that is free takes the oldest pending request's kind and every later pending request
+ * of that kind, in arrival order, while the batch's input stays within max_batch_bytes (0: 1 GiB) and the device
+ * bytes held by all workers stay within hbm_budget (0: no limit). Workers keep their buffers resident between
+ * batches and give them back when a pending batch could not be admitted otherwise; a request that cannot fit the
+ * budget even alone fails with -2. A request's result equals that of kolmo_sais_bwt_aux / kolmo_sais_unbwt_aux on
+ * the same arguments, whatever else shares its batch. Calls are thread-safe. */
+typedef struct kgbwt_server kgbwt_server;
+#define KGBWT_REQ_FWD 1 /* in = T (n bytes), out = U (n bytes), idx = I ((n-1)/r+1 entries, written), r = 2^k >= 2 */
+#define KGBWT_REQ_INV 2 /* in = U (n bytes), out = T (n bytes), idx = I (read), r = 2^k >= 2 or r = n */
+typedef struct {
+    int64_t submitted, completed, failed, cancelled, batches;
+    uint64_t bytes;      /* input bytes of the completed requests */
+    uint64_t hbm_in_use; /* device bytes held by the workers now (reservations of running batches included) */
+    uint64_t hbm_peak;
+} kgbwt_server_stats;
+kgbwt_server *kgbwt_server_create(int32_t slots, uint64_t hbm_budget, uint64_t max_batch_bytes);
+/* Stops the workers after their running batches; pending requests end with -3 (cancelled). */
+void kgbwt_server_destroy(kgbwt_server *s);
+/* Queues one request; the host buffers must stay valid until it completes. Returns its id (>= 0) or -1. */
+int64_t kgbwt_server_submit(kgbwt_server *s, int32_t kind, const uint8_t *in, uint8_t *out, int32_t *idx, int32_t n,
+                            int32_t r);
+/* Waits for request `id` (timeout_ms < 0: no limit). Returns 1 when it completed (*rc: 0, -1, -2 or -3 cancelled;
+ * *latency_us: submission to completion; the id is then forgotten), 0 on timeout, -1 for an unknown id. */
+int32_t kgbwt_server_wait(kgbwt_server *s, int64_t id, int32_t timeout_ms, int32_t *rc, double *latency_us);
+/* Cancels a request that has not started: 0, or -1 when it is running, done or unknown. */
+int32_t kgbwt_server_cancel(kgbwt_server *s, int64_t id);
+int32_t kgbwt_server_stats_read(kgbwt_server *s, kgbwt_server_stats *st);
+/* Test hook: the next `batches` batches fail as if their device allocation had failed (-2), without running. */
+int32_t kgbwt_server_inject_oom(kgbwt_server *s, int32_t batches);
+/* The batching policy on its own (host only): kinds[], n[], r[] of the pending requests in arrival order, the
+ * worker's current forward / inverse workspace bytes and the device bytes it may hold after the batch. Writes the
+ * indexes of the requests it would batch to take[] and returns their number (0: the oldest does not fit). */
+int32_t kgbwt_server_plan(const int32_t *kinds, const int32_t *n, const int32_t *r, int32_t count, uint64_t have_fwd,
+                          uint64_t have_inv, uint64_t avail, uint64_t max_batch_bytes, int32_t *take);
+/* Device bytes a worker with no workspace needs for one batch of these requests (host only). */
+uint64_t kgbwt_estimate_bytes(int32_t kind, const int32_t *n, const int32_t *r, int32_t count);
+
 /* ---- misc --------------------------------------------------------------------------------------------------------- */
 const char *kgbwt_last_error(void); /* text of the last error on this thread ("" if none) */
 int32_t kgbwt_version(void);

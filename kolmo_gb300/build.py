@@ -15,7 +15,7 @@ OUT = os.path.join(PKG, "_native")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["fwd.cu", "inv.cu", "api.cu"]
+CUDA_UNITS = ["fwd.cu", "inv.cu", "api.cu", "serve.cu"]
 LIB = os.path.join(OUT, "libkgbwt.so")
 LIB_CHECKED = os.path.join(OUT, "libkgbwt_checked.so")
 WORKLOADS = os.path.join(OUT, "libkgbwt_workloads.so")
@@ -76,7 +76,7 @@ def build_cuda(force: bool = False, extra: list[str] | None = None, verbose_ptxa
     with cf.ThreadPoolExecutor(max_workers=len(CUDA_UNITS)) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not _newer(lib, objs):
-        _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart"])
+        _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lpthread"])
     return lib
 
 

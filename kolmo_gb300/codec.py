@@ -170,3 +170,89 @@ class Engine:
 
     def workspace_bytes(self) -> int:
         return int(native.lib().kgbwt_engine_workspace_bytes(self.h))
+
+
+class Server:
+    """The request server (kgbwt_server_*): forward and inverse BWT requests on host arrays, batched as they arrive
+    onto `slots` workers with their own streams, admitted against an HBM budget (0: none)."""
+
+    def __init__(self, slots: int = 2, hbm_budget: int = 0, max_batch_bytes: int = 0):
+        self.h = native.lib().kgbwt_server_create(slots, hbm_budget, max_batch_bytes)
+        if not self.h:
+            raise RuntimeError("kgbwt_server_create failed")
+        self._keep = {}
+
+    def submit_fwd(self, T, r: int):
+        """Queues the forward BWT of T with sampling interval r; returns (id, U, I) (filled on completion)."""
+        T = _u8(T)
+        n = int(T.size)
+        U = np.zeros(max(n, 1), np.uint8)
+        I = np.zeros(max(n_samples(n, r), 1), np.int32)
+        rid = int(native.lib().kgbwt_server_submit(self.h, native.REQ_FWD, T.ctypes.data, U.ctypes.data,
+                                                   I.ctypes.data, n, r))
+        if rid < 0:
+            raise ValueError("bad forward request")
+        self._keep[rid] = (T, U, I)
+        return rid, U[:n], I[: n_samples(n, r)]
+
+    def submit_inv(self, U, r: int, I):
+        """Queues the inverse BWT of U (sampled indexes I, interval r); returns (id, T) (filled on completion)."""
+        U = _u8(U)
+        n = int(U.size)
+        Ib = np.ascontiguousarray(I, dtype=np.int32)
+        out = np.zeros(max(n, 1), np.uint8)
+        rid = int(native.lib().kgbwt_server_submit(self.h, native.REQ_INV, U.ctypes.data, out.ctypes.data,
+                                                   Ib.ctypes.data, n, r))
+        if rid < 0:
+            raise ValueError("bad inverse request")
+        self._keep[rid] = (U, Ib, out)
+        return rid, out[:n]
+
+    def wait(self, rid: int, timeout_ms: int = -1):
+        """Returns (status, rc, latency_us): status 1 done, 0 timeout, -1 unknown id."""
+        rc, lat = ctypes.c_int32(0), ctypes.c_double(0.0)
+        st = int(native.lib().kgbwt_server_wait(self.h, rid, timeout_ms, ctypes.byref(rc), ctypes.byref(lat)))
+        if st == 1:
+            self._keep.pop(rid, None)
+        return st, int(rc.value), float(lat.value)
+
+    def cancel(self, rid: int) -> int:
+        return int(native.lib().kgbwt_server_cancel(self.h, rid))
+
+    def inject_oom(self, batches: int) -> int:
+        return int(native.lib().kgbwt_server_inject_oom(self.h, batches))
+
+    def stats(self) -> dict:
+        s = native.ServerStats()
+        native.lib().kgbwt_server_stats_read(self.h, ctypes.byref(s))
+        return {f: getattr(s, f) for f, _ in native.ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            native.lib().kgbwt_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def server_plan(kinds, sizes, rs, have_fwd: int, have_inv: int, avail: int, max_batch_bytes: int = 0):
+    """The server's batching policy on its own: indexes of the pending requests it would batch next."""
+    k = np.ascontiguousarray(kinds, np.int32)
+    n = np.ascontiguousarray(sizes, np.int32)
+    r = np.ascontiguousarray(rs, np.int32)
+    take = np.zeros(max(len(k), 1), np.int32)
+    c = native.lib().kgbwt_server_plan(k.ctypes.data, n.ctypes.data, r.ctypes.data, len(k), have_fwd, have_inv,
+                                       avail, max_batch_bytes, take.ctypes.data)
+    return list(take[:c]) if c >= 0 else None
+
+
+def estimate_bytes(kind: int, sizes, rs) -> int:
+    """Device bytes a fresh worker needs for one batch of these requests."""
+    n = np.ascontiguousarray(sizes, np.int32)
+    r = np.ascontiguousarray(rs, np.int32)
+    return int(native.lib().kgbwt_estimate_bytes(kind, n.ctypes.data, r.ctypes.data, len(n)))

@@ -8,8 +8,7 @@
 #include <mutex>
 #include <vector>
 
-#include "fwd.cuh"
-#include "inv.cuh"
+#include "worker.cuh"
 
 namespace kgb {
 
@@ -34,56 +33,48 @@ int record_cuda_error(cudaError_t e, const char *what, const char *file, int lin
     return -2;
 }
 
-// Pinned host staging, grown on demand.
-struct Pinned {
-    u8 *p = nullptr;
-    size_t cap = 0;
-    int need(size_t bytes) {
-        if (bytes <= cap) return 0;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = bytes + bytes / 4 + 4096;
-        KGB_CHECK(cudaMallocHost(&p, want));
-        cap = want;
-        return 0;
-    }
-    ~Pinned() { if (p) cudaFreeHost(p); }
-};
+int Pinned::need(size_t bytes) {
+    if (bytes <= cap) return 0;
+    release();
+    size_t want = bytes + bytes / 4 + 4096;
+    KGB_CHECK(cudaMallocHost(&p, want));
+    cap = want;
+    return 0;
+}
+void Pinned::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+}
 
-}  // namespace kgb
+int Worker::init() {
+    if (stream) return 0;
+    KGB_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    return 0;
+}
+void Worker::release() {
+    eng.fwd.~FwdEngine();
+    new (&eng.fwd) FwdEngine();
+    eng.inv.~InvEngine();
+    new (&eng.inv) InvEngine();
+    stage_L.release();
+    stage_I.release();
+}
+Worker::~Worker() {
+    if (stream) cudaStreamDestroy(stream);
+}
 
-struct kgbwt_engine {
-    kgb::FwdEngine fwd;
-    kgb::InvEngine inv;
-    cudaStream_t last = nullptr;
-    int last_kind = 0;
-    std::vector<int> inv_status;
-    std::mutex mu;
-};
-
-namespace kgb {
-
-// The default context used by the drop-in and batch calls: one engine, one stream, pinned staging, one lock.
+// The default worker of the drop-in and batch calls, behind one lock.
 struct Context {
     std::mutex mu;
-    kgbwt_engine eng;
-    cudaStream_t stream = nullptr;
-    Pinned stage_L, stage_I;
-    bool ready = false;
-    int init() {
-        if (ready) return 0;
-        KGB_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        ready = true;
-        return 0;
-    }
+    Worker w;
 };
 static Context &ctx() {
     static Context *c = new Context();  // never destroyed: callers may run at process exit
     return *c;
 }
 
-static bool bad_r(int32_t r) { return r < 2 || (r & (r - 1)) != 0; }
+bool bad_r(int32_t r) { return r < 2 || (r & (r - 1)) != 0; }
 
 // KGBWT_PLAIN=1 in the environment makes the drop-in and batch calls use the plain path (debugging aid).
 static uint32_t env_flags() {
@@ -92,9 +83,7 @@ static uint32_t env_flags() {
     return plain ? KGBWT_PLAIN : 0u;
 }
 
-static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
-    Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
+int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
     std::vector<int> dev;
     std::vector<u32> n, r;
     for (int i = 0; i < count; i++) {
@@ -152,9 +141,7 @@ static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
     return 0;
 }
 
-static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
-    Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
+int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
     std::vector<int> dev;
     std::vector<u32> n, p0;
     for (int i = 0; i < count; i++) {
@@ -202,6 +189,17 @@ static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
         memcpy(j.U, C.stage_L.p + E.offsets()[k], (size_t)j.n);
     }
     return first;
+}
+
+static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    return run_fwd_jobs(C.w, jobs, count, flags);
+}
+static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    return run_inv_jobs(C.w, jobs, count, flags);
 }
 
 }  // namespace kgb

@@ -1538,15 +1538,10 @@ void FwdEngine::free_all() {
     Bcap = Icap = 0;
 }
 
-int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
-    if (ncap <= Ncap && bcap <= Bcap && icap <= Icap && (!want_sa || sa_cap)) return 0;
-    ncap = std::max<u64>(ncap, Ncap);
-    bcap = std::max<u32>(bcap, Bcap);
-    icap = std::max<u32>(icap, Icap);
-    want_sa = want_sa || sa_cap;
-    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
-    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
-    if (pool) { cudaFree(pool); pool = nullptr; }
+// The workspace of n text bytes, bcap blocks and icap sampled indexes: every device array in pool order. `add`
+// receives each array's address field and size (the estimate below only sums the sizes).
+template <typename Add>
+void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     const u64 n = ncap;
     const u32 smax = (u32)cfg.tile_cap / 2;
     const u64 nseg_small = n / 2 + bcap + 8;
@@ -1556,19 +1551,14 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     // lists), besides one group per block in the tile path's round 0; the keyed list takes any bucket size
     const u64 nseg_s = n / (GMED + 1) + bcap + 8;
     const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
-    struct Item { void **p; size_t bytes; };
-    std::vector<Item> items;
-    auto add = [&](void **p, size_t bytes) { items.push_back({p, align_up(std::max<size_t>(bytes, 16), 256)}); };
     add((void **)&own_T, n + 64);
     add((void **)&own_L, n + bcap + 64);
     add((void **)&own_I, (size_t)icap * 4 + 16);
-    own_SA = nullptr;
     if (want_sa) add((void **)&own_SA, n * 4);
     add((void **)&d_isa[0], n * 4);
     add((void **)&d_isa[1], n * 4);
     add((void **)&d_blk, (size_t)bcap * sizeof(BlockInfo));
     for (int l = 0; l < NLISTS; l++) {
-        lists[l] = ListView{nullptr, nullptr, nullptr, nullptr};
         add((void **)&lists[l].eid, n * 4);
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
@@ -1601,6 +1591,38 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     add((void **)&d_ltile, 64);
     add((void **)&d_segagg, stiles * 8 * 4);
     add((void **)&d_ctl, sizeof(Ctl));
+}
+
+u64 FwdEngine::estimate_bytes(u64 n, u32 bcap, u32 icap) {
+    u64 total = 0;
+    layout(std::max<u64>(n, Ncap), std::max<u32>(bcap, Bcap), std::max<u32>(icap, Icap), sa_cap,
+           [&](void **, size_t bytes) { total += align_up(std::max<size_t>(bytes, 16), 256); });
+    return total;
+}
+
+int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
+    if (ncap <= Ncap && bcap <= Bcap && icap <= Icap && (!want_sa || sa_cap)) return 0;
+    ncap = std::max<u64>(ncap, Ncap);
+    bcap = std::max<u32>(bcap, Bcap);
+    icap = std::max<u32>(icap, Icap);
+    want_sa = want_sa || sa_cap;
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (pool) { cudaFree(pool); pool = nullptr; }
+    own_SA = nullptr;
+    for (auto &l : lists) l = ListView{nullptr, nullptr, nullptr, nullptr};
+    struct Item { void **p; size_t bytes; };
+    std::vector<Item> items;
+    layout(ncap, bcap, icap, want_sa,
+           [&](void **p, size_t bytes) { items.push_back({p, align_up(std::max<size_t>(bytes, 16), 256)}); });
+    const u64 n = ncap;
+    const u32 smax = (u32)cfg.tile_cap / 2;
+    const u64 nseg_small = n / 2 + bcap + 8;
+    const u64 nseg_large = n / smax + bcap + 8;
+    const u64 nseg_med = n / (GTINY + 1) + bcap + 8;
+    const u64 nseg_s = n / (GMED + 1) + bcap + 8;
+    const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
+    const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
     size_t total = 0;
     for (auto &it : items) total += it.bytes;
     cudaError_t e = cudaMalloc(&pool, total);

@@ -102,6 +102,8 @@ class FwdEngine {
     const u32 *sa_dev() const { return d_SA; }
     int error_flag(cudaStream_t s, u32 *err);  // reads the device error word (after run)
     u64 workspace_bytes() const { return pool_bytes; }
+    // device bytes the workspace would hold after a call with these totals (no allocation; host only)
+    u64 estimate_bytes(u64 n, u32 blocks, u32 samples);
     FwdConfig cfg;
     FwdStats stats{};
     Profiler prof;  // plain path only: events around every launch when prof.on
@@ -113,6 +115,8 @@ class FwdEngine {
 
    private:
     int grow(u64 ncap, u32 bcap, u32 icap, bool want_sa);
+    template <typename Add>
+    void layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add);
     int run_plain(cudaStream_t s);
     int run_graph(cudaStream_t s);
     int build_graph(cudaStream_t s);

@@ -348,15 +348,9 @@ void InvEngine::free_all() {
     Ncap = Tcap = Ccap = 0; Bcap = 0;
 }
 
-int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
-    if (ncap <= Ncap && bcap <= Bcap && tcap <= Tcap && ccap <= Ccap) return 0;
-    ncap = std::max(ncap, Ncap); bcap = std::max(bcap, Bcap); tcap = std::max(tcap, Tcap); ccap = std::max(ccap, Ccap);
-    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
-    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
-    if (pool) { cudaFree(pool); pool = nullptr; }
-    struct Item { void **p; size_t bytes; };
-    std::vector<Item> items;
-    auto add = [&](void **p, size_t bytes) { items.push_back({p, ialign(std::max<size_t>(bytes, 16), 256)}); };
+// The workspace for ncap text bytes, bcap blocks, tcap psi-build chunks and ccap chain records, in pool order.
+template <typename Add>
+void InvEngine::layout(u64 ncap, u32 bcap, u64 tcap, u64 ccap, Add add) {
     add((void **)&own_U, ncap + 64);
     add((void **)&own_out, ncap + 64);
     add((void **)&d_psi, (ncap + bcap + 16) * 4);
@@ -374,6 +368,18 @@ int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
     add((void **)&d_dyn, (size_t)bcap * 4);
     add((void **)&d_status, (size_t)bcap * 4);
     add((void **)&d_chunks, (ccap / CHUNK + bcap + 8) * 12);
+}
+
+int InvEngine::grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap) {
+    if (ncap <= Ncap && bcap <= Bcap && tcap <= Tcap && ccap <= Ccap) return 0;
+    ncap = std::max(ncap, Ncap); bcap = std::max(bcap, Bcap); tcap = std::max(tcap, Tcap); ccap = std::max(ccap, Ccap);
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (pool) { cudaFree(pool); pool = nullptr; }
+    struct Item { void **p; size_t bytes; };
+    std::vector<Item> items;
+    layout(ncap, bcap, tcap, ccap,
+           [&](void **p, size_t bytes) { items.push_back({p, ialign(std::max<size_t>(bytes, 16), 256)}); });
     size_t total = 0;
     for (auto &it : items) total += it.bytes;
     cudaError_t e = cudaMalloc(&pool, total);
@@ -431,6 +437,22 @@ static int plan_layout(const u32 *off, const u32 *n, const u32 *p0, int count, s
         if (nchunk_all > 0xFFFF0000ull || nchains > 0xFFFF0000ull) return -1;
     }
     return 0;
+}
+
+u64 InvEngine::estimate_bytes(const u32 *n, int count) {
+    std::vector<u32> off(count), p0(count, 1);
+    u64 o = 0;
+    for (int b = 0; b < count; b++) { off[b] = (u32)o; o += ((u64)n[b] + 15) / 16 * 16; }
+    std::vector<InvBlock> blk;
+    std::vector<u32> cblk, chunks;
+    u64 nch = 0, nchains_ = 0;
+    u32 maxc = 0;
+    if (plan_layout(off.data(), n, p0.data(), count, blk, cblk, chunks, nch, nchains_, maxc)) return ~0ull;
+    u64 total = 0;
+    layout(std::max<u64>(o, Ncap), std::max<u32>((u32)count, Bcap), std::max<u64>(nch, Tcap),
+           std::max<u64>(nchains_, Ccap),
+           [&](void **, size_t bytes) { total += ialign(std::max<size_t>(bytes, 16), 256); });
+    return total;
 }
 
 int InvEngine::plan(const u32 *n, const u32 *p0, int count) {

@@ -43,9 +43,13 @@ class InvEngine {
     Profiler prof;  // plain path only
     bool prof_run = false;
     u64 workspace_bytes() const { return pool_bytes; }
+    // device bytes the workspace would hold after a call on blocks of these lengths (no allocation; host only)
+    u64 estimate_bytes(const u32 *n, int count);
 
    private:
     int grow(u64 ncap, u32 bcap, u64 tcap, u64 ccap);
+    template <typename Add>
+    void layout(u64 ncap, u32 bcap, u64 tcap, u64 ccap, Add add);
     int build_graph(cudaStream_t s);
     int enqueue(cudaStream_t s, long long *launches);
     void free_all();

@@ -41,6 +41,14 @@ PLAIN = 1
 OPT_SMALL_GROUP = 1
 OPT_WARP_PATH = 2
 OPT_LSD_ROUND0 = 3
+REQ_FWD = 1
+REQ_INV = 2
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("cancelled", ctypes.c_int64), ("batches", ctypes.c_int64), ("bytes", ctypes.c_uint64),
+                ("hbm_in_use", ctypes.c_uint64), ("hbm_peak", ctypes.c_uint64)]
 
 _lib = None
 
@@ -92,6 +100,24 @@ def lib():
     L.kgbwt_kernel_name.restype = ctypes.c_char_p
     L.kgbwt_unbwt_noalloc.argtypes = [_P, _P, _I32, _I32, _P]
     L.kgbwt_unbwt_noalloc.restype = _I32
+    L.kgbwt_server_create.argtypes = [_I32, ctypes.c_uint64, ctypes.c_uint64]
+    L.kgbwt_server_create.restype = _P
+    L.kgbwt_server_destroy.argtypes = [_P]
+    L.kgbwt_server_submit.argtypes = [_P, _I32, _P, _P, _P, _I32, _I32]
+    L.kgbwt_server_submit.restype = ctypes.c_int64
+    L.kgbwt_server_wait.argtypes = [_P, ctypes.c_int64, _I32, _P, _P]
+    L.kgbwt_server_wait.restype = _I32
+    L.kgbwt_server_cancel.argtypes = [_P, ctypes.c_int64]
+    L.kgbwt_server_cancel.restype = _I32
+    L.kgbwt_server_stats_read.argtypes = [_P, ctypes.POINTER(ServerStats)]
+    L.kgbwt_server_stats_read.restype = _I32
+    L.kgbwt_server_inject_oom.argtypes = [_P, _I32]
+    L.kgbwt_server_inject_oom.restype = _I32
+    L.kgbwt_server_plan.argtypes = [_P, _P, _P, _I32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                    ctypes.c_uint64, _P]
+    L.kgbwt_server_plan.restype = _I32
+    L.kgbwt_estimate_bytes.argtypes = [_I32, _P, _P, _I32]
+    L.kgbwt_estimate_bytes.restype = ctypes.c_uint64
     L.kgbwt_last_error.restype = ctypes.c_char_p
     L.kgbwt_version.restype = _I32
     _lib = L
@@ -108,5 +134,7 @@ EXPORTS = (
     "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
     "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
     "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_option",
-    "kgbwt_unbwt_noalloc",
+    "kgbwt_unbwt_noalloc", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
+    "kgbwt_server_cancel", "kgbwt_server_stats_read", "kgbwt_server_inject_oom", "kgbwt_server_plan",
+    "kgbwt_estimate_bytes",
 )
