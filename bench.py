@@ -190,8 +190,11 @@ def algorithmic_bytes(rec: dict) -> float:
     round 0 33 B per suffix, the inverse 10 B per byte over its passes (psi build: read L, write psi; walk: read psi,
     write text)."""
     k, e = rec["kernel"], rec["elems"]
-    if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed"):
+    if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed", "group_thread",
+             "group_warp"):
         return 48.0 * e
+    if k == "lsd_pass":
+        return 3.0 * e   # round 0 sorts every suffix once: its 24 B (key, id) read+write spread over 8 byte passes
     if k in ("tile_sort_prefix", "tile_sort_prefix_keyed", "tile_warp_prefix", "tile_warp_prefix_keyed"):
         return 33.0 * e
     if k == "inv_walk":
@@ -314,7 +317,9 @@ def run_ours(args, world, rank, local):
     for rec in prof_f:
         rr = rounds.setdefault(rec["round"], {"ms": 0.0, "m": 0})
         rr["ms"] += rec["ms"]
-        if rec["kernel"].startswith(("tile_sort", "tile_warp")):
+        # active suffixes of a rank round: the small, tiny and medium lists (their sort kernels) and the large list
+        # (keygen); the keyed tiles sort buckets of the large list and are not counted again
+        if rec["kernel"] in ("tile_sort_rank", "tile_warp_rank", "group_thread", "group_warp", "keygen"):
             rr["m"] += rec["elems"]
     round_table = []
     for j in sorted(rounds):
