@@ -95,6 +95,19 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
 #define KGBWT_OPT_WARP_PATH 2
 #define KGBWT_OPT_LSD_ROUND0 3
 int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value);
+/* The configuration the engine's last forward call ran with: tile_cap, tile_ctas, msd_ctas, small_group, warp_path,
+ * lsd_round0 (cfg[0..5]). Fields the caller set with kgbwt_engine_config / kgbwt_engine_option are used as set; the
+ * others come from the tuning table for the call's batch size when one is loaded, else the defaults. */
+int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg);
+/* Tuning table (no counterpart in the reference): configurations by batch size, a JSON file written by
+ * kolmo_gb300/autotune.py ({"buckets": [{"max_bytes": ..., "tile_ctas": ..., "msd_ctas": ..., "small_group": ...,
+ * "warp_path": ..., "lsd_round0": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes, else the
+ * last). Loaded on first use from $KGBWT_TUNING ("off": none), else from tuning_gb300.json in the package directory.
+ * kgbwt_tuning_load replaces it (NULL: no table) and returns the number of buckets or -1; kgbwt_tuning_lookup writes
+ * the configuration a batch of n bytes would get (as kgbwt_engine_last_config) and returns 1 when it came from the
+ * table, 0 for the defaults. */
+int32_t kgbwt_tuning_load(const char *path);
+int32_t kgbwt_tuning_lookup(uint64_t n, int32_t *cfg);
 /* Forward: text blocks in dT (16 readable bytes past the last block). Results: dL receives each block's L column
  * with its sentinel row (n + 1 bytes at off + block index; row p0 holds no text byte), dI the sampled indexes at
  * iout (dI[iout] = primary index), dSA (may be NULL) the suffix array at off. */

@@ -76,7 +76,7 @@ def build_cuda(force: bool = False, extra: list[str] | None = None, verbose_ptxa
     with cf.ThreadPoolExecutor(max_workers=len(CUDA_UNITS)) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not _newer(lib, objs):
-        _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lpthread"])
+        _run([nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart", "-lpthread", "-ldl"])
     return lib
 
 

@@ -168,8 +168,29 @@ class Engine:
         return [{"kernel": L.kgbwt_kernel_name(r.kernel).decode(), "round": r.round, "pass": r.pass_,
                  "elems": r.elems, "segs": r.segs, "ms": r.ms} for r in buf[:n]]
 
+    def last_config(self) -> dict:
+        """The configuration the last forward call ran with (caller settings over the tuning table)."""
+        c = np.zeros(6, np.int32)
+        native.lib().kgbwt_engine_last_config(self.h, c.ctypes.data)
+        return dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
+
     def workspace_bytes(self) -> int:
         return int(native.lib().kgbwt_engine_workspace_bytes(self.h))
+
+
+CONFIG_FIELDS = ("tile_cap", "tile_ctas", "msd_ctas", "small_group", "warp_path", "lsd_round0")
+
+
+def tuning_load(path) -> int:
+    """Replaces the tuning table (None: no table); returns the number of buckets or -1."""
+    return int(native.lib().kgbwt_tuning_load(None if path is None else str(path).encode()))
+
+
+def tuning_lookup(n: int):
+    """(from_table, config) that a batch of n bytes would run with."""
+    c = np.zeros(6, np.int32)
+    t = int(native.lib().kgbwt_tuning_lookup(n, c.ctypes.data))
+    return t == 1, dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
 
 
 class Server:

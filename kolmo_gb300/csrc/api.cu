@@ -2,10 +2,14 @@
 // device-buffer engines. See include/kgbwt.h for the contract of every function.
 #include "kgbwt.h"
 
+#include <dlfcn.h>
+
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "worker.cuh"
@@ -191,6 +195,115 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
     return first;
 }
 
+// ---- tuning table: configurations by batch size, written by kolmo_gb300/autotune.py as JSON
+// {"buckets": [{"max_bytes": B, "tile_ctas": ..., "msd_ctas": ..., "small_group": ..., "warp_path": ...,
+// "lsd_round0": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes (else the last).
+struct TuneBucket {
+    u64 max_bytes;
+    FwdConfig c;
+};
+static std::mutex g_tune_mu;
+static std::vector<TuneBucket> g_tune;
+static bool g_tune_tried = false;
+
+static const char *skip_ws(const char *p) {
+    while (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r') p++;
+    return p;
+}
+
+// Parses the bucket objects of a tuning file. Returns the number of buckets, or -1 when the text is not a tuning
+// table (no "buckets" array, a bucket without max_bytes, or a value out of range).
+static int parse_tuning(const char *text, std::vector<TuneBucket> &out) {
+    out.clear();
+    const char *p = strstr(text, "\"buckets\"");
+    if (!p) return -1;
+    p = strchr(p, '[');
+    if (!p) return -1;
+    p++;
+    for (;;) {
+        p = skip_ws(p);
+        if (*p == ',') { p++; continue; }
+        if (*p == ']') break;
+        if (*p != '{') return -1;
+        p++;
+        TuneBucket b{0, FwdConfig()};
+        bool have_max = false;
+        for (;;) {
+            p = skip_ws(p);
+            if (*p == ',') { p++; continue; }
+            if (*p == '}') { p++; break; }
+            if (*p != '"') return -1;
+            const char *k0 = ++p;
+            while (*p && *p != '"') p++;
+            if (!*p) return -1;
+            std::string key(k0, p - k0);
+            p = skip_ws(p + 1);
+            if (*p != ':') return -1;
+            p = skip_ws(p + 1);
+            if (*p == '"') {  // string value (a note): skip
+                p++;
+                while (*p && *p != '"') p++;
+                if (!*p) return -1;
+                p++;
+                continue;
+            }
+            char *e = nullptr;
+            const double v = strtod(p, &e);
+            if (e == p) return -1;
+            p = e;
+            if (key == "max_bytes") { if (v < 0) return -1; b.max_bytes = (u64)v; have_max = true; }
+            else if (key == "tile_ctas") { if (v < 1 || v > 8) return -1; b.c.tile_ctas = (int)v; }
+            else if (key == "msd_ctas") { if (v < 1 || v > 16) return -1; b.c.msd_ctas = (int)v; }
+            else if (key == "small_group") { if (v < 0 || v > 1024) return -1; b.c.small_group = (int)v; }
+            else if (key == "warp_path") { if (v != 0 && v != 1) return -1; b.c.warp_path = (int)v; }
+            else if (key == "lsd_round0") { if (v != 0 && v != 1) return -1; b.c.lsd_round0 = (int)v; }
+        }
+        if (!have_max) return -1;
+        out.push_back(b);
+    }
+    std::sort(out.begin(), out.end(), [](const TuneBucket &a, const TuneBucket &b) { return a.max_bytes < b.max_bytes; });
+    return (int)out.size();
+}
+
+static int load_tuning_file(const char *path, std::vector<TuneBucket> &out) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    std::string text;
+    char buf[4096];
+    size_t k;
+    while ((k = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, k);
+    fclose(f);
+    return parse_tuning(text.c_str(), out);
+}
+
+// First use: KGBWT_TUNING=<path> (or "off"), else the table shipped beside the package (../tuning_gb300.json
+// relative to this library's directory), else none.
+static void tune_autoload() {
+    if (g_tune_tried) return;
+    g_tune_tried = true;
+    const char *env = getenv("KGBWT_TUNING");
+    if (env && !strcmp(env, "off")) return;
+    if (env && *env) { if (load_tuning_file(env, g_tune) < 0) g_tune.clear(); return; }
+    Dl_info info;
+    if (dladdr((void *)&kgbwt_version, &info) && info.dli_fname) {
+        std::string p(info.dli_fname);
+        const size_t slash = p.rfind('/');
+        p = (slash == std::string::npos ? std::string(".") : p.substr(0, slash)) + "/../tuning_gb300.json";
+        if (load_tuning_file(p.c_str(), g_tune) < 0) g_tune.clear();
+    }
+}
+
+bool tuned_config(u64 n, FwdConfig *out) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_autoload();
+    if (g_tune.empty()) return false;
+    const TuneBucket *b = &g_tune.back();
+    for (const TuneBucket &t : g_tune)
+        if (n <= t.max_bytes) { b = &t; break; }
+    *out = b->c;
+    return true;
+}
+
 static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
@@ -254,14 +367,18 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
     if (tile_cap && tile_cap != 4096 && tile_cap != 8192) return -1;
     if (tile_ctas < 0 || tile_ctas > 8 || msd_ctas < 0 || msd_ctas > 16) return -1;
     std::lock_guard<std::mutex> lock(e->mu);
-    if (tile_cap && tile_cap != e->fwd.cfg.tile_cap) {
+    if (tile_cap && tile_cap != e->fwd.ucfg.tile_cap) {
         // a different tile capacity changes list capacities: drop the workspace (it is rebuilt on the next call)
+        const FwdConfig keep = e->fwd.ucfg;
+        const u32 mask = e->fwd.cfg_explicit;
         e->fwd.~FwdEngine();
         new (&e->fwd) FwdEngine();
-        e->fwd.cfg.tile_cap = tile_cap;
+        e->fwd.ucfg = keep;
+        e->fwd.cfg_explicit = mask;
+        e->fwd.ucfg.tile_cap = tile_cap;
     }
-    if (tile_ctas) e->fwd.cfg.tile_ctas = tile_ctas;
-    if (msd_ctas) e->fwd.cfg.msd_ctas = msd_ctas;
+    if (tile_ctas) { e->fwd.ucfg.tile_ctas = tile_ctas; e->fwd.cfg_explicit |= CFG_TILE_CTAS; }
+    if (msd_ctas) { e->fwd.ucfg.msd_ctas = msd_ctas; e->fwd.cfg_explicit |= CFG_MSD_CTAS; }
     return 0;
 }
 
@@ -271,15 +388,18 @@ int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
     switch (option) {
         case KGBWT_OPT_SMALL_GROUP:
             if (value < 0 || value > 1024) return -1;
-            e->fwd.cfg.small_group = value;
+            e->fwd.ucfg.small_group = value;
+            e->fwd.cfg_explicit |= CFG_SMALL_GROUP;
             return 0;
         case KGBWT_OPT_WARP_PATH:
             if (value != 0 && value != 1) return -1;
-            e->fwd.cfg.warp_path = value;
+            e->fwd.ucfg.warp_path = value;
+            e->fwd.cfg_explicit |= CFG_WARP_PATH;
             return 0;
         case KGBWT_OPT_LSD_ROUND0:
             if (value != 0 && value != 1) return -1;
-            e->fwd.cfg.lsd_round0 = value;
+            e->fwd.ucfg.lsd_round0 = value;
+            e->fwd.cfg_explicit |= CFG_LSD_ROUND0;
             return 0;
         default:
             return -1;
@@ -381,6 +501,35 @@ int32_t kgbwt_engine_profile_read(kgbwt_engine *e, kgbwt_prof *out, int32_t cap)
 }
 
 const char *kgbwt_kernel_name(int32_t kernel) { return kernel_name(kernel); }
+
+int32_t kgbwt_tuning_load(const char *path) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_tried = true;  // an explicit load (or clear) replaces the automatic one
+    if (!path) { g_tune.clear(); return 0; }
+    std::vector<TuneBucket> t;
+    const int k = load_tuning_file(path, t);
+    if (k < 0) { record_error("kgbwt_tuning_load: not a readable tuning table"); return -1; }
+    g_tune.swap(t);
+    return k;
+}
+
+int32_t kgbwt_tuning_lookup(uint64_t n, int32_t *cfg) {
+    if (!cfg) return -1;
+    FwdConfig c;
+    const bool t = tuned_config(n, &c);
+    cfg[0] = c.tile_cap; cfg[1] = c.tile_ctas; cfg[2] = c.msd_ctas; cfg[3] = c.small_group; cfg[4] = c.warp_path;
+    cfg[5] = c.lsd_round0;
+    return t ? 1 : 0;
+}
+
+int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg) {
+    if (!e || !cfg) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    const FwdConfig &c = e->fwd.cfg;
+    cfg[0] = c.tile_cap; cfg[1] = c.tile_ctas; cfg[2] = c.msd_ctas; cfg[3] = c.small_group; cfg[4] = c.warp_path;
+    cfg[5] = c.lsd_round0;
+    return 0;
+}
 
 const char *kgbwt_last_error(void) { return g_err; }
 int32_t kgbwt_version(void) { return 100; }

@@ -1689,6 +1689,7 @@ int FwdEngine::plan(const u32 *n, const u32 *r, int count, bool want_sa) {
     N = off; B = (u32)count; nI = (u32)io;
     ext = false;
     want_sa_run = want_sa;
+    resolve_config();
     int rc = grow(N, B, nI, want_sa);
     if (rc) return rc;
     d_T = own_T; d_L = own_L; d_I = own_I; d_SA = want_sa ? own_SA : nullptr;
@@ -1711,10 +1712,22 @@ int FwdEngine::plan_external(const u32 *off, const u32 *n, const u32 *r, const u
     N = end; B = (u32)count; nI = (u32)io;
     ext = true;
     want_sa_run = dSA != nullptr;
+    resolve_config();
     int rc = grow(N, B, 0, false);
     if (rc) return rc;
     d_T = dT; d_L = dL; d_I = dI; d_SA = dSA;
     return 0;
+}
+
+void FwdEngine::resolve_config() {
+    cfg = ucfg;
+    FwdConfig t;
+    if (!tuned_config(N, &t)) return;
+    if (!(cfg_explicit & CFG_TILE_CTAS)) cfg.tile_ctas = t.tile_ctas;
+    if (!(cfg_explicit & CFG_MSD_CTAS)) cfg.msd_ctas = t.msd_ctas;
+    if (!(cfg_explicit & CFG_SMALL_GROUP)) cfg.small_group = t.small_group;
+    if (!(cfg_explicit & CFG_WARP_PATH)) cfg.warp_path = t.warp_path;
+    if (!(cfg_explicit & CFG_LSD_ROUND0)) cfg.lsd_round0 = t.lsd_round0;
 }
 
 static int ceil_log2(u64 x) { int k = 0; while ((1ull << k) < x) k++; return k; }
@@ -2216,10 +2229,8 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan
     if (int rc = setup_round0(s)) return rc;
     if (!use_graph) return run_plain(s);
-    const u64 key = ((u64)B << 40) ^ ((u64)N << 2) ^ ((u64)(uintptr_t)d_T) ^ ((u64)(uintptr_t)d_L << 1) ^
-                    ((u64)(uintptr_t)d_I << 3) ^ ((u64)(uintptr_t)d_SA << 5) ^ (u64)cfg.tile_cap ^ ((u64)Ncap << 7) ^
-                    ((u64)lsd_enabled() << 63);
-    if (!gexec || key != graph_key) {
+    const GraphKey key{N, Ncap, B, d_T, d_L, d_I, d_SA, cfg, lsd_enabled()};
+    if (!gexec || !(key == graph_key)) {
         // capture on the engine's own stream: the caller's may be the legacy default stream, which cannot capture
         if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
         if (int rc = build_graph(cap_stream)) return rc;

@@ -71,6 +71,11 @@ struct FwdConfig {
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
     int lsd_round0 = 1;   // round 0 (8-byte prefixes) as one LSD radix sort of all suffixes; 0: bucket passes + tiles
 };
+// Fields of FwdConfig a caller set explicitly (they override the tuning table).
+enum : u32 { CFG_TILE_CTAS = 1, CFG_MSD_CTAS = 2, CFG_SMALL_GROUP = 4, CFG_WARP_PATH = 8, CFG_LSD_ROUND0 = 16 };
+// The tuning table's configuration for a batch of n text bytes: fills the fields the table sets (tile_ctas,
+// msd_ctas, small_group, warp_path, lsd_round0) and returns true, or returns false when no table is loaded.
+bool tuned_config(u64 n, FwdConfig *out);
 
 struct FwdStats {
     int rounds;
@@ -82,6 +87,9 @@ struct FwdStats {
 // Device buffers for batches up to (ncap bytes, bcap blocks). Reused across calls; grown on demand.
 class FwdEngine {
    public:
+    FwdConfig ucfg;         // the caller's configuration (api: kgbwt_engine_config / _option)
+    u32 cfg_explicit = 0;   // CFG_* bits of the fields the caller set
+    void resolve_config();  // cfg = ucfg, with the tuning table's values for the fields the caller left alone
     FwdEngine();
     ~FwdEngine();
     // Prepares a batch of `count` blocks with lengths n[] (each >= 2) and sampling intervals r[]: lays the blocks
@@ -104,7 +112,7 @@ class FwdEngine {
     u64 workspace_bytes() const { return pool_bytes; }
     // device bytes the workspace would hold after a call with these totals (no allocation; host only)
     u64 estimate_bytes(u64 n, u32 blocks, u32 samples);
-    FwdConfig cfg;
+    FwdConfig cfg;          // the configuration of the current call
     FwdStats stats{};
     Profiler prof;  // plain path only: events around every launch when prof.on
 
@@ -165,7 +173,21 @@ class FwdEngine {
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t cap_stream = nullptr;
     int graph_cap_key = 0;
-    u64 graph_key = 0;
+    // everything a captured graph depends on: pointers, sizes and the configuration it was captured with
+    struct GraphKey {
+        u64 N, Ncap;
+        u32 B;
+        const void *T, *L, *I, *SA;
+        FwdConfig cfg;
+        bool lsd;
+        bool operator==(const GraphKey &o) const {
+            return N == o.N && Ncap == o.Ncap && B == o.B && T == o.T && L == o.L && I == o.I && SA == o.SA &&
+                   cfg.tile_cap == o.cfg.tile_cap && cfg.tile_ctas == o.cfg.tile_ctas &&
+                   cfg.msd_ctas == o.cfg.msd_ctas && cfg.small_group == o.cfg.small_group &&
+                   cfg.warp_path == o.cfg.warp_path && cfg.lsd_round0 == o.cfg.lsd_round0 && lsd == o.lsd;
+        }
+    };
+    GraphKey graph_key{};
     int sm_count = 0;
     int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0, grid_warp = 0, grid_lsd = 0;
 };

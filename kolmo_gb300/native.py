@@ -118,6 +118,12 @@ def lib():
     L.kgbwt_server_plan.restype = _I32
     L.kgbwt_estimate_bytes.argtypes = [_I32, _P, _P, _I32]
     L.kgbwt_estimate_bytes.restype = ctypes.c_uint64
+    L.kgbwt_engine_last_config.argtypes = [_P, _P]
+    L.kgbwt_engine_last_config.restype = _I32
+    L.kgbwt_tuning_load.argtypes = [ctypes.c_char_p]
+    L.kgbwt_tuning_load.restype = _I32
+    L.kgbwt_tuning_lookup.argtypes = [ctypes.c_uint64, _P]
+    L.kgbwt_tuning_lookup.restype = _I32
     L.kgbwt_last_error.restype = ctypes.c_char_p
     L.kgbwt_version.restype = _I32
     _lib = L
@@ -136,5 +142,5 @@ EXPORTS = (
     "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_option",
     "kgbwt_unbwt_noalloc", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
     "kgbwt_server_cancel", "kgbwt_server_stats_read", "kgbwt_server_inject_oom", "kgbwt_server_plan",
-    "kgbwt_estimate_bytes",
+    "kgbwt_estimate_bytes", "kgbwt_engine_last_config", "kgbwt_tuning_load", "kgbwt_tuning_lookup",
 )

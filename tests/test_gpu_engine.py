@@ -120,3 +120,38 @@ def test_round0_paths_on_mixed_batch(lsd_round0):
             col = L[off + b: off + b + t.size + 1]
             p0 = int(oI[0])
             assert np.array_equal(np.concatenate([col[:p0], col[p0 + 1:]]), oU), b
+
+
+def test_tuning_table_applies_and_explicit_settings_win(tmp_path):
+    import json
+    import os
+
+    import torch
+
+    t = W.zipf_prose(2 << 20, 21)
+    n = t.size
+    dT = torch.zeros(n + 64, dtype=torch.uint8, device="cuda")
+    dT[:n] = torch.from_numpy(t).cuda()
+    table = {"buckets": [{"max_bytes": 1 << 40, "tile_ctas": 1, "msd_ctas": 3, "small_group": 0, "warp_path": 0,
+                          "lsd_round0": 0}]}
+    p = tmp_path / "tune.json"
+    p.write_text(json.dumps(table))
+    pkg = os.path.join(os.path.dirname(codec.__file__), "tuning_gb300.json")
+    try:
+        assert codec.tuning_load(p) == 1
+        outs = []
+        for explicit in (False, True):
+            eng = codec.Engine()
+            if explicit:
+                eng.config(0, 2, 8, 64, 1, 1)
+            dL = torch.zeros(n + 1, dtype=torch.uint8, device="cuda")
+            dI = torch.zeros(4, dtype=torch.int32, device="cuda")
+            assert eng.fwd(dT, dL, dI, [(0, n, 1 << 20, 0)]) == 0 and eng.wait()[0] == 0
+            c = eng.last_config()
+            want = (2, 8, 64, 1, 1) if explicit else (1, 3, 0, 0, 0)
+            assert (c["tile_ctas"], c["msd_ctas"], c["small_group"], c["warp_path"], c["lsd_round0"]) == want
+            outs.append((dL.cpu().numpy(), dI.cpu().numpy()))
+            eng.close()
+        assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    finally:
+        codec.tuning_load(pkg if os.path.exists(pkg) else None)

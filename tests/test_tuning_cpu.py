@@ -1,0 +1,59 @@
+"""The tuning table without a GPU: the library parses the autotuner's JSON, picks the bucket of a batch size, rejects
+malformed tables, and reports the defaults when no table is loaded."""
+import json
+import os
+
+import pytest
+
+from kolmo_gb300 import codec
+
+PKG_TABLE = os.path.join(os.path.dirname(codec.__file__), "tuning_gb300.json")
+
+
+@pytest.fixture
+def restore_table():
+    yield
+    codec.tuning_load(PKG_TABLE if os.path.exists(PKG_TABLE) else None)
+
+
+def test_bucket_lookup(tmp_path, restore_table):
+    t = {"version": 1, "device": "test", "buckets": [
+        {"max_bytes": 1 << 30, "tile_ctas": 2, "msd_ctas": 4, "small_group": 0, "warp_path": 1, "lsd_round0": 0,
+         "workload": "large"},
+        {"max_bytes": 1 << 20, "tile_ctas": 1, "msd_ctas": 8, "small_group": 64, "warp_path": 0, "lsd_round0": 1,
+         "fwd_ms": 0.5},
+    ]}
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(t))
+    assert codec.tuning_load(p) == 2
+    hit, c = codec.tuning_lookup(1000)
+    assert hit and c["tile_ctas"] == 1 and c["msd_ctas"] == 8 and c["warp_path"] == 0 and c["lsd_round0"] == 1
+    hit, c = codec.tuning_lookup(5 << 20)
+    assert hit and c["tile_ctas"] == 2 and c["msd_ctas"] == 4 and c["small_group"] == 0 and c["lsd_round0"] == 0
+    hit, c = codec.tuning_lookup(1 << 33)  # past every bucket: the last one
+    assert hit and c["msd_ctas"] == 4
+    assert c["tile_cap"] == 4096  # never tuned
+
+
+def test_malformed_tables_are_refused(tmp_path, restore_table):
+    for bad in ('{"no": []}', '{"buckets": [{"tile_ctas": 2}]}', '{"buckets": [{"max_bytes": 10, "msd_ctas": 99}]}',
+                '{"buckets": [{"max_bytes": 10, "warp_path": 2}]}', 'not json'):
+        p = tmp_path / "bad.json"
+        p.write_text(bad)
+        assert codec.tuning_load(p) == -1
+    assert codec.tuning_load(tmp_path / "missing.json") == -1
+
+
+def test_no_table_gives_defaults(restore_table):
+    assert codec.tuning_load(None) == 0
+    hit, c = codec.tuning_lookup(64 << 20)
+    assert not hit and c == {"tile_cap": 4096, "tile_ctas": 2, "msd_ctas": 8, "small_group": 64, "warp_path": 1,
+                             "lsd_round0": 1}
+
+
+def test_packaged_table_parses_if_present(restore_table):
+    if not os.path.exists(PKG_TABLE):
+        pytest.skip("no packaged table")
+    with open(PKG_TABLE) as f:
+        n = len(json.load(f)["buckets"])
+    assert codec.tuning_load(PKG_TABLE) == n
