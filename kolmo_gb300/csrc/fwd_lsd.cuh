@@ -473,53 +473,71 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
         u32 tidx = (u32)(base[3] >> 32) + (u32)xt, te = (u32)base[3] + (u32)(xt >> 32);
         u32 midx = (u32)(base[4] >> 32) + (u32)xm, me = (u32)base[4] + (u32)(xm >> 32);
         u32 carry = ch.carry0;
-        for (int j = 0; j < SEG_IPT; j++) {
-            u32 p, gf; bool ok, st, en;
-            seg_step(v, ch, j, carry, p, ok, st, en, gf);
-            if (!ok || !en) continue;
-            const u32 len = p - gf + 1;
-            const u32 b = v.has_hi ? v.hi[p] : 0u;
-            const u32 head = gf - a.blk[b].soff;
-            if (len == 1) {
-                resolve(a, isa_nxt, v.val[p], head, b, res, r1++);
-                continue;
+        constexpr int QB = 8;  // positions per phase: group ends first, then their loads, then the writes
+        for (int j0 = 0; j0 < SEG_IPT; j0 += QB) {
+            u32 pv[QB], gfv[QB], live = 0;
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                u32 p, gf; bool ok, st, en;
+                seg_step(v, ch, j0 + q, carry, p, ok, st, en, gf);
+                pv[q] = p; gfv[q] = gf;
+                if (ok && en) live |= 1u << q;
             }
-            Seg g;
-            g.len = len; g.head = head; g.bd = b;
-            if (len <= GTINY) {
-                g.start = te;
-                KGB_GUARD(tidx < a.cap_segt && (u64)te + len <= a.cap_n, &c->err, E_SEG) {
-                    tl_.seg[tidx] = g;
-                    v.gbase[gf] = te;
-                    v.gidx[gf] = tidx | GRP_TINY;
+            u32 bv[QB], idv[QB];
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                if (!((live >> q) & 1)) continue;
+                bv[q] = v.has_hi ? __ldg(v.hi + pv[q]) : 0u;
+                idv[q] = pv[q] == gfv[q] ? __ldg(v.val + pv[q]) : 0u;  // ids of finished suffixes (groups of one)
+            }
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                if (!((live >> q) & 1)) continue;
+                const u32 p = pv[q], gf = gfv[q];
+                const u32 len = p - gf + 1;
+                const u32 b = bv[q];
+                const u32 head = gf - a.blk[b].soff;
+                if (len == 1) {
+                    resolve(a, isa_nxt, idv[q], head, b, res, r1++);
+                    continue;
                 }
-                tidx++; te += len;
-            } else if (len <= GMED) {
-                g.start = me;
-                KGB_GUARD(midx < a.cap_segm && (u64)me + len <= a.cap_n, &c->err, E_SEG) {
-                    ml_.seg[midx] = g;
-                    v.gbase[gf] = me;
-                    v.gidx[gf] = midx | GRP_MED;
+                Seg g;
+                g.len = len; g.head = head; g.bd = b;
+                if (len <= GTINY) {
+                    g.start = te;
+                    KGB_GUARD(tidx < a.cap_segt && (u64)te + len <= a.cap_n, &c->err, E_SEG) {
+                        tl_.seg[tidx] = g;
+                        v.gbase[gf] = te;
+                        v.gidx[gf] = tidx | GRP_TINY;
+                    }
+                    tidx++; te += len;
+                } else if (len <= GMED) {
+                    g.start = me;
+                    KGB_GUARD(midx < a.cap_segm && (u64)me + len <= a.cap_n, &c->err, E_SEG) {
+                        ml_.seg[midx] = g;
+                        v.gbase[gf] = me;
+                        v.gidx[gf] = midx | GRP_MED;
+                    }
+                    midx++; me += len;
+                } else if (len <= TS) {
+                    g.start = se;
+                    KGB_GUARD(sidx < a.cap_segs && (u64)se + len <= a.cap_n, &c->err, E_SEG) {
+                        sl.seg[sidx] = g;
+                        write_tmap_small(a, sl.tmap, TS, se, len, sidx);
+                        if (len > WARP_GROUP) sl.tbig[se / TS] = round + 1;
+                        v.gbase[gf] = se;
+                        v.gidx[gf] = sidx;
+                    }
+                    sidx++; se += len;
+                } else {
+                    g.start = le;
+                    KGB_GUARD(lidx < a.cap_segl && (u64)le + len <= a.cap_n, &c->err, E_SEG) {
+                        ll.seg[lidx] = g;
+                        v.gbase[gf] = le;
+                        v.gidx[gf] = lidx | GRP_LARGE;
+                    }
+                    lidx++; le += len;
                 }
-                midx++; me += len;
-            } else if (len <= TS) {
-                g.start = se;
-                KGB_GUARD(sidx < a.cap_segs && (u64)se + len <= a.cap_n, &c->err, E_SEG) {
-                    sl.seg[sidx] = g;
-                    write_tmap_small(a, sl.tmap, TS, se, len, sidx);
-                    if (len > WARP_GROUP) sl.tbig[se / TS] = round + 1;
-                    v.gbase[gf] = se;
-                    v.gidx[gf] = sidx;
-                }
-                sidx++; se += len;
-            } else {
-                g.start = le;
-                KGB_GUARD(lidx < a.cap_segl && (u64)le + len <= a.cap_n, &c->err, E_SEG) {
-                    ll.seg[lidx] = g;
-                    v.gbase[gf] = le;
-                    v.gidx[gf] = lidx | GRP_LARGE;
-                }
-                lidx++; le += len;
             }
         }
         __syncthreads();
@@ -537,31 +555,48 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
     const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
     u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
+    constexpr int QB = 8;  // positions per phase: group starts first, then every load, then every store
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const SegChunk ch = seg_chunk(a, v, t, wl);
         u32 carry = ch.carry0;
-        for (int j = 0; j < SEG_IPT; j++) {
-            u32 p, gf; bool ok, st, en;
-            seg_step(v, ch, j, carry, p, ok, st, en, gf);
-            if (!ok || (st && en)) continue;  // groups of one were resolved by part 1
-            const u32 b = v.has_hi ? v.hi[p] : 0u;
-            const u32 id = v.val[p];
-            const u32 head = gf - a.blk[b].soff;
-            const u32 gi = v.gidx[gf];
-            const u32 slot = v.gbase[gf] + (p - gf);
-            KGB_GUARD(id < a.cap_n && slot < a.cap_n, &c->err, E_LIST) {
-                isa_nxt[id] = head;
-                if (gi & GRP_LARGE) {
-                    ll.eid[slot] = id;
-                    if (slot % TSM == 0) {
-                        KGB_GUARD(slot / TSM < a.cap_tml, &c->err, E_TMAP) ll.tmap[slot / TSM] = gi & ~GRP_LARGE;
+        for (int j0 = 0; j0 < SEG_IPT; j0 += QB) {
+            u32 pv[QB], gfv[QB], live = 0;
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                u32 p, gf; bool ok, st, en;
+                seg_step(v, ch, j0 + q, carry, p, ok, st, en, gf);
+                pv[q] = p; gfv[q] = gf;
+                if (ok && !(st && en)) live |= 1u << q;  // groups of one were resolved by part 1
+            }
+            u32 idv[QB], giv[QB], gbv[QB], bv[QB];
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                if (!((live >> q) & 1)) continue;
+                idv[q] = __ldg(v.val + pv[q]);
+                bv[q] = v.has_hi ? __ldg(v.hi + pv[q]) : 0u;
+                giv[q] = __ldg(v.gidx + gfv[q]);
+                gbv[q] = __ldg(v.gbase + gfv[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < QB; q++) {
+                if (!((live >> q) & 1)) continue;
+                const u32 id = idv[q], gi = giv[q], p = pv[q], gf = gfv[q];
+                const u32 head = gf - a.blk[bv[q]].soff;
+                const u32 slot = gbv[q] + (p - gf);
+                KGB_GUARD(id < a.cap_n && slot < a.cap_n, &c->err, E_LIST) {
+                    isa_nxt[id] = head;
+                    if (gi & GRP_LARGE) {
+                        ll.eid[slot] = id;
+                        if (slot % TSM == 0) {
+                            KGB_GUARD(slot / TSM < a.cap_tml, &c->err, E_TMAP) ll.tmap[slot / TSM] = gi & ~GRP_LARGE;
+                        }
+                    } else if (gi & GRP_TINY) {
+                        tl_.eid[slot] = id;
+                    } else if (gi & GRP_MED) {
+                        ml_.eid[slot] = id;
+                    } else {
+                        sl.eid[slot] = id;
                     }
-                } else if (gi & GRP_TINY) {
-                    tl_.eid[slot] = id;
-                } else if (gi & GRP_MED) {
-                    ml_.eid[slot] = id;
-                } else {
-                    sl.eid[slot] = id;
                 }
             }
         }
