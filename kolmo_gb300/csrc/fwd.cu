@@ -119,6 +119,15 @@ __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, 
     res.ekey[ridx] = p;
 }
 
+// Tiny groups keep their ids in one array for the whole sort (a tiny group only shrinks, so its members never move to
+// another list): a producer takes `elems` fresh slots there and `groups` descriptors in the next round's tiny list.
+// Returns (first slot, first descriptor).
+__device__ __forceinline__ uint2 alloc_tiny(Ctl *c, u32 rpar, u32 groups, u32 elems) {
+    const u32 e = atomicAdd(&c->p_alloc, elems);
+    const u64 o = atomicAdd(&c->cnt[L_P0 + (rpar ^ 1)], ((u64)groups << 32) | elems);
+    return make_uint2(e, (u32)(o >> 32));
+}
+
 // ------------------------------------------------------------------------------------------------ tile sorter
 // Tile t of a small-group list covers every segment whose start lies in [t * TS, (t + 1) * TS) (TS = TILE / 2 =
 // SMAX, so a tile holds at most TILE elements). tmap[t] = index of the first such segment; the producers of a
@@ -425,9 +434,9 @@ __global__ void __launch_bounds__(TPB, TileTraits<PREFIX, TILE>::MINB) k_tile_so
                 S.bases[1] = (u32)(o >> 32);
             }
             if (tot_p) {
-                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)tot_gp << 32) | tot_p);
-                S.pbases[0] = (u32)o;
-                S.pbases[1] = (u32)(o >> 32);
+                const uint2 o = alloc_tiny(a.ctl, rpar, tot_gp, tot_p);
+                S.pbases[0] = o.x;
+                S.pbases[1] = o.y;
             }
             if (tot_m) {
                 const u64 o = atomicAdd(&a.ctl->cnt[L_M0 + (rpar ^ 1)], ((u64)tot_gm << 32) | tot_m);
@@ -703,8 +712,8 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
                 ebase = (u32)o; sbase = (u32)(o >> 32);
             }
             if (np) {
-                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)ngp << 32) | np);
-                pebase = (u32)o; psbase = (u32)(o >> 32);
+                const uint2 o = alloc_tiny(a.ctl, rpar, ngp, np);
+                pebase = o.x; psbase = o.y;
             }
             if (nres) rbase = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)nres);
         }
@@ -796,15 +805,17 @@ __device__ __forceinline__ void cswap(u32 &ka, u32 &va, u32 &kb, u32 &vb) {
 __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
     const Ctl *ctl = a.ctl;
     const u32 rpar = ctl->rpar, h = ctl->h;
+    // in and out share the id array: a group's ids stay in its slots; only descriptors move to the next list
     const ListView in = a.lists[L_P0 + rpar], out = a.lists[L_P0 + (rpar ^ 1)], res = a.lists[L_R0 + rpar];
     const u64 c = ctl->cnt[L_P0 + rpar];
-    const u32 nelem = (u32)c, nseg = (u32)(c >> 32);
-    if (nelem > a.cap_n || nseg > a.cap_segt) {
+    const u32 nseg = (u32)(c >> 32), nslots = ctl->p_alloc;
+    if ((u32)c > a.cap_n || nseg > a.cap_segt || nslots > a.cap_n) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctl->err, E_LIST);
         return;
     }
     const u32 *isa_cur = a.isa[rpar];
     u32 *isa_nxt = a.isa[rpar ^ 1];
+    u32 *ids = in.eid;
     const u32 lane = lane_id();
     for (u32 base = blockIdx.x * TPB; base < nseg; base += gridDim.x * TPB) {
         const u32 s = base + threadIdx.x;
@@ -812,7 +823,7 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         Seg g = {0, 0, 0, 0};
         if (ok) g = in.seg[s];
         u32 len = g.len;
-        if (len > GTINY || (u64)g.start + len > nelem) {  // broken list invariant: report, never overrun
+        if (len > GTINY || (u64)g.start + len > nslots) {  // broken list invariant: report, never overrun
             atomicOr(&a.ctl->err, E_SEG);
             len = 0;
         }
@@ -820,7 +831,7 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         const u64 end = len ? blk_end(a, b) : 0;
         u32 k[GTINY], v[GTINY];
 #pragma unroll
-        for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? in.eid[g.start + q] : 0u;
+        for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? ids[g.start + q] : 0u;
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++) k[q] = q < len ? rank_key(isa_cur, v[q], h, end) : 0xFFFFFFFFu;
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
@@ -847,21 +858,24 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
             else { ns++; ng += st; }
         }
         const bool unsplit = ng == 1 && ns == len;  // one run covers the group
-        const u32 pk = ns | (ng << 10) | (n1 << 20);  // each at most GTINY per thread: warp totals <= 256
+        const u32 pk = ng | (n1 << 16);  // each at most GTINY per thread: warp totals <= 256
         const u32 incl = warp_incl_sum(pk), tot = __shfl_sync(0xffffffffu, incl, 31), excl = incl - pk;
-        u32 ebase = 0, sbase = 0, rbase = 0;
+        const u32 ts = warp_sum(ns);
+        u32 sbase = 0, rbase = 0;
         if (lane == 0) {
-            const u32 ts = tot & 0x3FF, tg = (tot >> 10) & 0x3FF, t1 = tot >> 20;
-            if (ts) {
-                const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)tg << 32) | ts);
-                ebase = (u32)o; sbase = (u32)(o >> 32);
-            }
+            const u32 tg = tot & 0xFFFF, t1 = tot >> 16;
+            if (tg) sbase = (u32)(atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)tg << 32) | ts) >> 32);
             if (t1) rbase = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)t1);
         }
-        u32 e = __shfl_sync(0xffffffffu, ebase, 0) + (excl & 0x3FF);
-        u32 gi = __shfl_sync(0xffffffffu, sbase, 0) + ((excl >> 10) & 0x3FF);
-        u32 r = __shfl_sync(0xffffffffu, rbase, 0) + (excl >> 20);
+        u32 gi = __shfl_sync(0xffffffffu, sbase, 0) + (excl & 0xFFFF);
+        u32 r = __shfl_sync(0xffffffffu, rbase, 0) + (excl >> 16);
         const bool skip_rank = (g.bd & STABLE) && unsplit;
+        // a group that split is rewritten in sorted order, so that each surviving run is contiguous in its slots
+        if (!unsplit && len) {
+#pragma unroll
+            for (u32 q = 0; q < GTINY; q++)
+                if (q < len) ids[g.start + q] = v[q];
+        }
         u32 rs = 0;  // first position of the current run
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++) {
@@ -877,11 +891,9 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
             if (!skip_rank) {
                 KGB_GUARD(v[q] < a.cap_n, &a.ctl->err, E_RANK) isa_nxt[v[q]] = head;
             }
-            KGB_GUARD(e < a.cap_n, &a.ctl->err, E_LIST) out.eid[e] = v[q];
-            e++;
             if (en) {
                 Seg ng_;
-                ng_.len = q - rs + 1; ng_.start = e - ng_.len; ng_.head = head;
+                ng_.len = q - rs + 1; ng_.start = g.start + rs; ng_.head = head;
                 ng_.bd = b | (unsplit ? STABLE : 0u);
                 KGB_GUARD(gi < a.cap_segt, &a.ctl->err, E_SEG) out.seg[gi] = ng_;
                 gi++;
@@ -1024,7 +1036,7 @@ __global__ void __launch_bounds__(TPB) k_group_warp(FwdArgs a) {
         }
         u32 pb = 0, psb = 0, mb = 0, msb = 0, rb = 0;
         if (lane == 0) {
-            if (off_p) { const u64 o = atomicAdd(&a.ctl->cnt[L_P0 + (rpar ^ 1)], ((u64)g_p << 32) | off_p); pb = (u32)o; psb = (u32)(o >> 32); }
+            if (off_p) { const uint2 o = alloc_tiny(a.ctl, rpar, g_p, off_p); pb = o.x; psb = o.y; }
             if (off_m) { const u64 o = atomicAdd(&a.ctl->cnt[L_M0 + (rpar ^ 1)], ((u64)g_m << 32) | off_m); mb = (u32)o; msb = (u32)(o >> 32); }
             if (n1) rb = (u32)atomicAdd(&a.ctl->cnt[L_R0 + rpar], (u64)n1);
         }
@@ -1559,7 +1571,7 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_isa[1], n * 4);
     add((void **)&d_blk, (size_t)bcap * sizeof(BlockInfo));
     for (int l = 0; l < NLISTS; l++) {
-        add((void **)&lists[l].eid, n * 4);
+        if (l != L_P1) add((void **)&lists[l].eid, n * 4);  // the two tiny lists share one id array
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
         const bool tiny = l == L_P0 || l == L_P1, med = l == L_M0 || l == L_M1;
@@ -1635,6 +1647,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     pool_bytes = total;
     size_t off = 0;
     for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
+    lists[L_P1].eid = lists[L_P0].eid;
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemset(lists[l].tbig, 0xFF, ntm_small * 4));
     // orand rows start as (or = 0, and = ~0)

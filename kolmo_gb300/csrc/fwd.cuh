@@ -29,7 +29,7 @@ enum : u32 {
     L_K0, L_K1,  // bucket-pass work lists (ping-pong across passes)
     L_KS,        // small buckets produced by the bucket passes, keys attached
     L_R0, L_R1,  // suffixes resolved in a round (their ranks are copied to the other rank buffer next round)
-    L_P0, L_P1,  // tiny groups (2..GTINY elements) of the rank rounds, one list per round parity
+    L_P0, L_P1,  // tiny groups (2..GTINY elements) of the rank rounds: descriptors per round parity, ids in one array
     L_M0, L_M1,  // medium groups (GTINY+1..GMED elements) of the rank rounds, one list per round parity
     NLISTS
 };
@@ -61,6 +61,7 @@ struct Ctl {
     u32 vary_hi, and_hi;
     u32 m;              // suffixes sorted
     u32 seq;            // call sequence number (tags the look-back words of the radix passes)
+    u32 p_alloc;        // slots taken so far in the tiny-group id array (shared by both parities, never reused)
 };
 
 struct FwdConfig {

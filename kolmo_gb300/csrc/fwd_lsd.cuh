@@ -461,7 +461,12 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
         u64 xm = block_excl_sum64(cm, ws[3], &tm);
         if (threadIdx.x == 0) {
             base[4] = (u32)tm ? atomicAdd(&c->cnt[L_M0 + (rpar ^ 1)], (tm << 32) | (tm >> 32)) : 0ull;
-            base[3] = (u32)tt ? atomicAdd(&c->cnt[L_P0 + (rpar ^ 1)], (tt << 32) | (tt >> 32)) : 0ull;
+            if ((u32)tt) {
+                const uint2 o = alloc_tiny(c, rpar, (u32)tt, (u32)(tt >> 32));
+                base[3] = ((u64)o.y << 32) | o.x;
+            } else {
+                base[3] = 0;
+            }
             base[0] = (ts & 0xFFFF) ? atomicAdd(&c->cnt[L_R0 + rpar], ts & 0xFFFF) : 0ull;
             base[1] = (ts >> 16) & 0xFFFF ? atomicAdd(&c->cnt[L_S0 + (rpar ^ 1)], (((ts >> 16) & 0xFFFF) << 32) | (ts >> 32)) : 0ull;
             base[2] = (u32)tl ? atomicAdd(&c->cnt[L_L0 + (rpar ^ 1)], (tl << 32) | (tl >> 32)) : 0ull;
