@@ -61,7 +61,6 @@ void Worker::release() {
     new (&eng.fwd) FwdEngine();
     eng.inv.~InvEngine();
     new (&eng.inv) InvEngine();
-    stage_L.release();
     stage_I.release();
 }
 Worker::~Worker() {
@@ -118,11 +117,11 @@ int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) 
     if (cudaMemsetAsync(E.text() + E.total(), 0, 64, s) != cudaSuccess)
         return fail(record_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__));
     if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
-    const size_t lbytes = E.total() + dev.size();
-    if ((rc = C.stage_L.need(lbytes)) || (rc = C.stage_I.need((size_t)E.samples() * 4))) return fail(rc);
-    if (cudaMemcpyAsync(C.stage_L.p, E.lcol(), lbytes, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(C.stage_I.p, E.samples_dev(), (size_t)E.samples() * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(result)", __FILE__, __LINE__));
+    // sampled indexes first (small), then each block's L column straight into the caller's U, without its sentinel
+    // row (two device-to-host copies per block once the primary index is known)
+    if ((rc = C.stage_I.need((size_t)E.samples() * 4))) return fail(rc);
+    if (cudaMemcpyAsync(C.stage_I.p, E.samples_dev(), (size_t)E.samples() * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(samples)", __FILE__, __LINE__));
     u32 err = 0;
     if ((rc = E.error_flag(s, &err))) return fail(rc);
     if (err) {
@@ -134,12 +133,20 @@ int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) 
     const u32 *I = reinterpret_cast<const u32 *>(C.stage_I.p);
     for (size_t k = 0; k < dev.size(); k++) {
         kgbwt_fwd_job &j = jobs[dev[k]];
-        const u8 *L = C.stage_L.p + E.offsets()[k] + k;
+        const u8 *L = E.lcol() + E.offsets()[k] + k;
+        const u32 p0 = I[E.iouts()[k]];
+        if (p0 < 1 || p0 > (u32)j.n) return fail(-2);
+        if ((p0 && cudaMemcpyAsync(j.U, L, p0, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+            ((u32)j.n > p0 && cudaMemcpyAsync(j.U + p0, L + p0 + 1, (size_t)j.n - p0, cudaMemcpyDeviceToHost, s) !=
+                                 cudaSuccess))
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(result)", __FILE__, __LINE__));
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaStreamSynchronize", __FILE__, __LINE__));
+    for (size_t k = 0; k < dev.size(); k++) {
+        kgbwt_fwd_job &j = jobs[dev[k]];
         const u32 *Ib = I + E.iouts()[k];
         const u32 ns = (u32)((j.n - 1) / j.r + 1);
-        const u32 p0 = Ib[0];
-        memcpy(j.U, L, p0);
-        memcpy(j.U + p0, L + p0 + 1, (size_t)j.n - p0);
         for (u32 t = 0; t < ns; t++) j.I[t] = (int32_t)Ib[t];
     }
     return 0;
@@ -177,9 +184,6 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
         if (cudaMemcpyAsync(E.input() + E.offsets()[k], jobs[dev[k]].T, n[k], cudaMemcpyHostToDevice, s) != cudaSuccess)
             return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(bwt)", __FILE__, __LINE__));
     if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
-    if ((rc = C.stage_L.need(E.total()))) return fail(rc);
-    if (cudaMemcpyAsync(C.stage_L.p, E.output(), E.total(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
     std::vector<int> st;
     if ((rc = E.fetch_status(s, st))) return fail(rc);
     int first = 0;
@@ -190,8 +194,12 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
             if (!first) { first = -1; record_error("inverse BWT: not a valid BWT string for its primary index"); }
             continue;
         }
-        memcpy(j.U, C.stage_L.p + E.offsets()[k], (size_t)j.n);
+        // the decoded text straight into the caller's buffer
+        if (cudaMemcpyAsync(j.U, E.output() + E.offsets()[k], (size_t)j.n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
     }
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(record_cuda_error(cudaGetLastError(), "cudaStreamSynchronize", __FILE__, __LINE__));
     return first;
 }
 
