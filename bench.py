@@ -184,6 +184,12 @@ def prose_block(rank: int, mib: int = 64):
     return W.zipf_prose(mib * MIB, W.SEED_PROSE_64MIB + rank)
 
 
+# DRAM bytes per unit (suffix) measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 16 MiB prose
+# case, one timed step: profiles/traffic_group_thread_lsd_pass_prose16.md. The 64 MiB launch's traffic is scaled by
+# the suffixes it processes.
+TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 7.3}
+
+
 def algorithmic_bytes(rec: dict) -> float:
     """Algorithmic bytes of one launch (the per-unit figures of the doubling model): a rank round costs 48 B per
     active suffix (read its id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id),
@@ -352,11 +358,11 @@ def run_ours(args, world, rank, local):
         "gpu_launches": args.steps * (launches_fwd + launches_inv),
         "clocks": clk,
     }
-    if traffic_path := os.environ.get("KGBWT_TRAFFIC_JSON"):
-        try:
-            out["roofline"]["traffic"] = json.load(open(traffic_path)).get(dom)
-        except Exception:
-            pass
+    if dom in TRAFFIC_PER_SUFFIX:
+        elems = sum(rec["elems"] for rec in prof if rec["kernel"] == dom) / max(dd["launches"], 1)
+        out["roofline"]["traffic"] = round(TRAFFIC_PER_SUFFIX[dom] * elems)
+        out["roofline"]["traffic_source"] = ("ncu dram bytes per suffix on the 16 MiB case x suffixes per launch "
+                                             "(profiles/traffic_group_thread_lsd_pass_prose16.md)")
     if rank == 0:
         kind, threads, cpu_v, reps = time_cpu(T[: 16 * MIB], r, budget_s=12.0)
         out["cpu_baseline"] = {"value": round(cpu_v, 2), "unit": "MiB/s", "cores": threads, "kind": kind,
