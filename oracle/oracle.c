@@ -17,6 +17,7 @@
  * The inverse is the LF walk of the reference's independent Python decoder (tests/bwt_reference.py:270-290).
  * Argument checks and return codes follow sais.c:12029-12038 and 12057-12068. */
 #include <stdint.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -164,6 +165,67 @@ int32_t orc_unbwt_aux(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32
     for (int32_t t = 0; t <= (n - 1) / r; t++) if (I[t] <= 0 || I[t] > n) return -1;
     return lf_walk(T, U, n, I[0], NULL);
 }
+/* Multi-threaded decode from the sampled indexes, as the reference's per-sample decoder does
+ * (libsais_unbwt_decode_omp, sais.c:10842-): I[t] (t >= 1) is the row of the suffix starting at t * r, so segment t
+ * [t*r, (t+1)*r) is produced by walking LF backwards from the row of suffix (t+1)*r (from row 0, the sentinel, for
+ * the last segment). Every segment is independent; `threads` workers take them in turn. The LF table is built once.
+ * Returns 0, -1 (arguments, as orc_unbwt_aux) or -2 (memory). */
+struct seg_job {
+    const uint8_t *U;
+    uint8_t *out;
+    const uint32_t *lf;
+    const int32_t *I;
+    int32_t n, r, idx, k, next, stride;
+};
+static void *seg_worker(void *arg) {
+    struct seg_job *J = (struct seg_job *)arg;
+    for (int32_t t = J->next; t <= J->k; t += J->stride) {
+        const int32_t lo = t * J->r, hi = t == J->k ? J->n : (t + 1) * J->r;
+        uint32_t row = t == J->k ? 0u : (uint32_t)J->I[t + 1];
+        for (int32_t j = hi - 1; j >= lo; j--) {
+            J->out[j] = row == (uint32_t)J->idx ? 0 : J->U[row - (row > (uint32_t)J->idx)];
+            row = J->lf[row];
+        }
+    }
+    return NULL;
+}
+int32_t orc_unbwt_aux_mt(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32_t r, const int32_t *I,
+                         int32_t threads) {
+    if (!T || !U || !A || n < 0 || ((r != n) && ((r < 2) || ((r & (r - 1)) != 0))) || !I) return -1;
+    if (n <= 1) { if (I[0] != n) return -1; if (n == 1) U[0] = T[0]; return 0; }
+    for (int32_t t = 0; t <= (n - 1) / r; t++) if (I[t] <= 0 || I[t] > n) return -1;
+    const int32_t k = (n - 1) / r, idx = I[0];
+    if (threads < 2 || k < 1) return lf_walk(T, U, n, idx, NULL);
+    uint32_t *lf = (uint32_t *)malloc(((size_t)n + 1) * sizeof(uint32_t));
+    uint8_t *tmp = (uint8_t *)malloc((size_t)n);
+    if (!lf || !tmp) { free(lf); free(tmp); return -2; }
+    uint32_t cnt[256] = {0}, base[256];
+    for (int32_t i = 0; i < n; i++) cnt[T[i]]++;
+    uint32_t s = 1;
+    for (int c = 0; c < 256; c++) { base[c] = s; s += cnt[c]; }
+    lf[idx] = 0;
+    for (int32_t q = 0; q <= n; q++) {
+        if (q == idx) continue;
+        lf[q] = base[T[q - (q > idx)]]++;
+    }
+    if (threads > k + 1) threads = k + 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+    struct seg_job *jobs = (struct seg_job *)malloc(sizeof(struct seg_job) * (size_t)threads);
+    if (!th || !jobs) { free(lf); free(tmp); free(th); free(jobs); return -2; }
+    char *live = (char *)calloc((size_t)threads, 1);
+    if (!live) { free(lf); free(tmp); free(th); free(jobs); return -2; }
+    for (int32_t w = 0; w < threads; w++) {
+        jobs[w] = (struct seg_job){T, tmp, lf, I, n, r, idx, k, w, threads};
+        if (pthread_create(&th[w], NULL, seg_worker, &jobs[w]) == 0) live[w] = 1;
+        else seg_worker(&jobs[w]);  /* no thread: decode its segments here */
+    }
+    for (int32_t w = 0; w < threads; w++) if (live[w]) pthread_join(th[w], NULL);
+    free(live);
+    memcpy(U, tmp, (size_t)n); /* T == U allowed */
+    free(lf); free(tmp); free(th); free(jobs);
+    return 0;
+}
+
 /* kolmo_sais_unbwt (sais.c:12079-12082) */
 int32_t orc_unbwt(const uint8_t *T, uint8_t *U, int32_t *A, int32_t n, int32_t i) {
     return orc_unbwt_aux(T, U, A, n, n, &i);

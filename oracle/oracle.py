@@ -49,6 +49,8 @@ def port_lib():
         lib.orc_bwt_aux.argtypes = [_P, _P, _P, _I32, _I32, _P]
         lib.orc_bwt_aux_sa.argtypes = [_P, _P, _P, _I32, _I32, _P, _P]
         lib.orc_unbwt_aux.argtypes = [_P, _P, _P, _I32, _I32, _P]
+        lib.orc_unbwt_aux_mt.argtypes = [_P, _P, _P, _I32, _I32, _P, _I32]
+        lib.orc_unbwt_aux_mt.restype = _I32
         lib.orc_unbwt.argtypes = [_P, _P, _P, _I32, _I32]
         lib.orc_sa.argtypes = [_P, _P, _I32]
         lib.orc_sa_from_bwt.argtypes = [_P, _I32, _I32, _P]
@@ -115,7 +117,8 @@ def unbwt_aux(U: np.ndarray, r: int, I: np.ndarray, use_ref: bool = False, threa
     if use_ref:
         rc = ref_lib().kolmo_sais_unbwt_aux(_ptr(Uc), _ptr(out), _ptr(A), n, r, _ptr(Ic), threads)
     else:
-        rc = port_lib().orc_unbwt_aux(_ptr(Uc), _ptr(out), _ptr(A), n, r, _ptr(Ic))
+        rc = (port_lib().orc_unbwt_aux_mt(_ptr(Uc), _ptr(out), _ptr(A), n, r, _ptr(Ic), threads) if threads > 1
+              else port_lib().orc_unbwt_aux(_ptr(Uc), _ptr(out), _ptr(A), n, r, _ptr(Ic)))
     return int(rc), out[:n]
 
 

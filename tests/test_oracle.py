@@ -106,3 +106,17 @@ def test_planted_mistake_is_caught(golden):
     U2[[10, 11]] = U2[[11, 10]]
     if U2[10] != U2[11]:
         assert h(U2) != c["U"]
+
+
+@pytest.mark.parametrize("n,r", [(2, 2), (100, 8), (4097, 512), (300_000, 1 << 12), (1 << 20, 1 << 17)])
+def test_threaded_decode_equals_serial(n, r):
+    """The restatement's multi-threaded per-sample decode (the CPU baseline's inverse) equals the serial LF walk."""
+    T = W.markov2(n, n % 1000 + 1)
+    rc, U, I = O.bwt_aux(T, r)
+    assert rc == 0
+    for threads in (1, 3, 8):
+        rc2, back = O.unbwt_aux(U, r, I, threads=threads)
+        assert rc2 == 0 and np.array_equal(back, T)
+    bad = I.copy()
+    bad[-1] = n + 1
+    assert O.unbwt_aux(U, r, bad, threads=4)[0] == -1
