@@ -1593,10 +1593,9 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
     const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
-    for (int q = 0; q < 2; q++) {
-        add((void **)&d_lval[q], n * 4);
-        add((void **)&d_lhi[q], n * 4);
-    }
+    // the round-0 radix buffers (ids and block indexes, ping-pong) alias the bucket-pass work lists K0 / K1: round 0
+    // on the LSD path runs no bucket pass, and in the rank rounds the medium-key scratch (lval[0]) is written after the
+    // round's bucket passes and read before the next round's
     add((void **)&d_lstat, ltiles * 256 * 8);
     add((void **)&d_segbits, n / 8 + 64);
     add((void **)&d_lhist, NSLOT * 256 * 4);
@@ -1648,6 +1647,8 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     size_t off = 0;
     for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
     lists[L_P1].eid = lists[L_P0].eid;
+    d_lval[0] = lists[L_K0].eid; d_lval[1] = lists[L_K0].ekey;
+    d_lhi[0] = lists[L_K1].eid; d_lhi[1] = lists[L_K1].ekey;
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemset(lists[l].tbig, 0xFF, ntm_small * 4));
     // orand rows start as (or = 0, and = ~0)
