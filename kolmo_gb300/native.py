@@ -54,6 +54,10 @@ _lib = None
 
 
 def lib_path() -> str:
+    """The library to load: $KGBWT_LIB when set (an explicit build, e.g. for side-by-side timing), else the
+    bounds-checked build when KGBWT_CHECKED=1, else the release build."""
+    if os.environ.get("KGBWT_LIB"):
+        return os.environ["KGBWT_LIB"]
     return _build.LIB_CHECKED if os.environ.get("KGBWT_CHECKED") == "1" else _build.LIB
 
 
