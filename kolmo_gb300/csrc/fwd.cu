@@ -66,6 +66,7 @@ struct FwdArgs {
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
     u32 *lval[2], *lhi[2], *segbits;
+    u32 *lkh[2], *lkl[2];  // round 0: the 8-byte keys carried with the ids (high / low halves)
     u64 *lstat;
     u32 *lhist, *ltile, *segagg;
     u32 spin_limit;
@@ -1593,9 +1594,10 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
     const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
-    // the round-0 radix buffers (ids and block indexes, ping-pong) alias the bucket-pass work lists K0 / K1: round 0
-    // on the LSD path runs no bucket pass, and in the rank rounds the medium-key scratch (lval[0]) is written after the
-    // round's bucket passes and read before the next round's
+    // the round-0 radix buffers (ids and block indexes, ping-pong) alias the bucket-pass work lists K0 / K1, and the
+    // key halves alias the large list L0 and the keyed small list KS: round 0 on the LSD path uses none of those lists,
+    // and in the rank rounds the medium-key scratch (lval[0]) is written after the round's bucket passes and read
+    // before the next round's
     add((void **)&d_lstat, ltiles * 256 * 8);
     add((void **)&d_segbits, n / 8 + 64);
     add((void **)&d_lhist, NSLOT * 256 * 4);
@@ -1676,6 +1678,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 void FwdEngine::set_caps(FwdArgs &a) const {
     a.orand64 = d_orand64;
     for (int q = 0; q < 2; q++) { a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
+    a.lkh[0] = lists[L_L0].eid; a.lkl[0] = lists[L_L0].ekey; a.lkh[1] = lists[L_KS].eid; a.lkl[1] = lists[L_KS].ekey;
     a.segbits = d_segbits;
     a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg;
     a.spin_limit = 1u << 22;

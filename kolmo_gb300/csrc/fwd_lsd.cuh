@@ -1,10 +1,10 @@
 // Round 0 of the forward sort as one LSD radix sort: every suffix of the batch is sorted by (block, zero-padded
 // 8-byte prefix) with one pass per varying key byte (single-pass scatter with decoupled look-back), then a
 // segmentation turns the sorted order into ranks, finished suffixes and the rank rounds' groups (the small-group list
-// for the tile kernels, the large-group list for the bucket passes). The passes move only suffix ids (and block
-// indexes when the batch has several blocks): a pass reads its digit, one text byte, from the text, which stays in L2
-// while the ids stream through. Included by fwd.cu inside namespace kgb, after the kernels it shares (FwdArgs,
-// resolve, tile-map writers).
+// for the tile kernels, the large-group list for the bucket passes). The passes move (key, id) items, the 8-byte key
+// as two 32-bit halves (and the block index when the batch has several blocks): a pass takes its digit from the key
+// it carries, and the segmentation compares neighbouring keys without touching the text. Included by fwd.cu inside
+// namespace kgb, after the kernels it shares (FwdArgs, resolve, tile-map writers).
 #pragma once
 // (included inside namespace kgb)
 
@@ -29,13 +29,6 @@ __device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte 
 }
 __device__ __forceinline__ bool lsd_has_hi(const FwdArgs &a) { return a.B > 1; }
 
-// Digit `slot` of suffix id of block b: slots 0..7 are the bytes of its zero-padded 8-byte prefix, least significant
-// (text byte id + 7) first; slots 8..11 are the bytes of the block index.
-__device__ __forceinline__ u32 lsd_digit(const u8 *__restrict__ T, u32 id, u32 b, u64 end, int slot) {
-    if (slot >= 8) return (b >> (8 * (slot - 8))) & 0xFFu;
-    const u32 d = 7 - slot;
-    return (u64)id + d < end ? (u32)__ldg(T + id + d) : 0u;
-}
 // The zero-padded 8-byte prefix of suffix id (block ending at end) as a big-endian word.
 __device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u32 id, u64 end) {
     u64 k = load_be64(T, id);
@@ -52,8 +45,9 @@ __global__ void k_lsd_begin(FwdArgs a) {
     if (threadIdx.x == 0) c->cnt[L_R0 + c->rpar] = 0;
 }
 
-// Suffix ids in the dense order of the batch (block index beside them when the batch has several blocks), and the
-// byte histogram of the whole text (row 0 of the histogram table), from which every pass's digit counts follow.
+// Suffix ids and their 8-byte keys in the dense order of the batch (block index beside them when the batch has
+// several blocks), and the byte histogram of the whole text (row 0 of the histogram table), from which every pass's
+// digit counts follow.
 __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
     __shared__ u32 hs[256];
     const bool hi = lsd_has_hi(a);
@@ -69,7 +63,10 @@ __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
             const u64 x = (u64)bi.soff + j;
             __stcs(a.lval[0] + x, id);
             if (hi) __stcs(a.lhi[0] + x, b);
-            atomicAdd(&hs[__ldg(a.T + id)], 1u);
+            const u64 k = lsd_key(a.T, id, (u64)bi.off + bi.n);
+            __stcs(a.lkh[0] + x, (u32)(k >> 32));
+            __stcs(a.lkl[0] + x, (u32)k);
+            atomicAdd(&hs[(u32)(k >> 56)], 1u);
         }
     }
     __syncthreads();
@@ -132,6 +129,7 @@ __global__ void k_lsd_hist0(FwdArgs a) {
 template <bool HI>
 struct LsdSmem {
     u32 val[LSD_TILE];
+    u32 kh[LSD_TILE], kl[LSD_TILE];
     u32 hi[HI ? LSD_TILE : 1];
     u8 dg[LSD_TILE];
     u16 wcnt[TPB / 32][256];
@@ -145,7 +143,7 @@ struct LsdSmem {
 // digit, publish the tile's digit counts, look back over earlier tiles for the global offsets (bounded spin), stage
 // the tile in shared memory in digit order and write it out in runs.
 template <bool HI>
-__global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slot) {
+__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LsdSmem<HI> &S = *reinterpret_cast<LsdSmem<HI> *>(smem_raw);
     const Ctl *c = a.ctl;
@@ -155,7 +153,6 @@ __global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slo
     const u32 m = c->m;
     const u32 ntiles = (m + LSD_TILE - 1) / LSD_TILE;
     const u64 epoch = (u64)((c->seq << 4) | (u32)slot) << 32;
-    const u64 end0 = blk_end(a, 0);
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
     // digit bases of the pass: exclusive scan of the slot's counts
@@ -169,21 +166,25 @@ __global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slo
     if (tile >= ntiles) return;
     const u32 base = tile * LSD_TILE;
     const u32 cnt = min((u32)LSD_TILE, m - base);
-    const u32 *vin = a.lval[par], *hin = a.lhi[par];
+    const u32 *vin = a.lval[par], *hin = a.lhi[par], *khin = a.lkh[par], *klin = a.lkl[par];
     // rk[j]: rank in the warp's digit bucket (bits 0..15) | digit, 0x100 past the end (bits 16..24)
-    u32 v[LSD_IPT], hh[LSD_IPT], rk[LSD_IPT];
+    u32 v[LSD_IPT], hh[LSD_IPT], rk[LSD_IPT], kh[LSD_IPT], kl[LSD_IPT];
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
         const bool ok = x < cnt;
         v[j] = ok ? __ldcs(vin + base + x) : 0u;
+        kh[j] = ok ? __ldcs(khin + base + x) : 0u;
+        kl[j] = ok ? __ldcs(klin + base + x) : 0u;
         hh[j] = ok && HI ? __ldcs(hin + base + x) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        const u64 end = HI ? blk_end(a, hh[j]) : end0;
-        rk[j] = (x < cnt ? lsd_digit(a.T, v[j], hh[j], end, slot) : 0x100u) << 16;
+        u32 d;
+        if (slot >= 8) d = (hh[j] >> (8 * (slot - 8))) & 0xFFu;
+        else d = ((slot < 4 ? kl[j] : kh[j]) >> (8 * (slot & 3))) & 0xFFu;
+        rk[j] = (x < cnt ? d : 0x100u) << 16;
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
@@ -217,6 +218,8 @@ __global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slo
         if (d < 256) {
             const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFFu);
             S.val[p] = v[j];
+            S.kh[p] = kh[j];
+            S.kl[p] = kl[j];
             if (HI) S.hi[p] = hh[j];
             S.dg[p] = (u8)d;
         }
@@ -257,11 +260,13 @@ __global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slo
     }
     S.gbase[tid] = S.dbase[tid] + excl - dstart;
     __syncthreads();
-    u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1];
+    u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1], *khout = a.lkh[par ^ 1], *klout = a.lkl[par ^ 1];
     for (u32 i = tid; i < cnt; i += TPB) {
         const u32 dst = S.gbase[S.dg[i]] + i;
         if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
             __stcs(vout + dst, S.val[i]);
+            __stcs(khout + dst, S.kh[i]);
+            __stcs(klout + dst, S.kl[i]);
             if (HI) __stcs(hout + dst, S.hi[i]);
         }
     }
@@ -271,7 +276,7 @@ __global__ void __launch_bounds__(TPB, HI ? 3 : 4) k_lsd_pass(FwdArgs a, int slo
 // Positions are handled in tiles of SEG_TILE; warp w of a tile owns the SEG_IPT * 32 consecutive positions starting at
 // tile base + w * 32 * SEG_IPT and visits them lane-striped (position = chunk base + j * 32 + lane), so every load is
 // coalesced. Group starts are kept as a bitmask (bit p of the mask: a group starts at position p), written by the
-// count kernel (which compares neighbouring prefixes read from the text); the emit kernels read only the bits.
+// count kernel (which compares neighbouring sorted keys); the emit kernels read only the bits.
 __device__ __forceinline__ u32 lsd_final_par(const Ctl *c) { return __popc(active_slots(c)) & 1; }
 
 struct SegBufs {
@@ -302,7 +307,6 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     const SegBufs v = seg_bufs(a);
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 lane = lane_id(), warp = warp_id();
-    const u64 end0 = blk_end(a, 0);
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
         u32 last = 0;
@@ -310,13 +314,15 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
         for (int j = 0; j < SEG_IPT; j++) {
             const u32 p = cb + j * 32 + lane;
             const bool ok = p < v.m;
+            const u32 fp = lsd_final_par(a.ctl);
+            const u32 *KH = a.lkh[fp], *KL = a.lkl[fp];
             u32 h = ok && v.has_hi ? v.hi[p] : 0u;
-            u64 k = ok ? lsd_key(a.T, v.val[p], v.has_hi ? blk_end(a, h) : end0) : 0ull;
+            u64 k = ok ? ((u64)KH[p] << 32) | KL[p] : 0ull;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1);
             u32 hp = __shfl_up_sync(0xffffffffu, h, 1);
             if (lane == 0 && ok && p > 0) {
                 hp = v.has_hi ? v.hi[p - 1] : 0u;
-                kp = lsd_key(a.T, v.val[p - 1], v.has_hi ? blk_end(a, hp) : end0);
+                kp = ((u64)KH[p - 1] << 32) | KL[p - 1];
             }
             const bool st = ok && (p == 0 || k != kp || h != hp);
             const u32 b = __ballot_sync(0xffffffffu, st);
