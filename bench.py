@@ -187,9 +187,9 @@ def prose_block(rank: int, mib: int = 64):
 
 
 # DRAM bytes per unit (suffix) measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 16 MiB prose
-# case, one timed step: profiles/traffic_group_thread_lsd_pass_prose16.md. The 64 MiB launch's traffic is scaled by
-# the suffixes it processes.
-TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 7.3}
+# case: profiles/traffic_group_thread_lsd_pass_prose16.md (tiny groups) and profiles/lsd_pass_keyed_prose16.md (the
+# keyed round-0 pass). The 64 MiB launch's traffic is scaled by the suffixes it processes.
+TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 22.5}
 
 
 def algorithmic_bytes(rec: dict) -> float:
@@ -363,8 +363,7 @@ def run_ours(args, world, rank, local):
     if dom in TRAFFIC_PER_SUFFIX:
         elems = sum(rec["elems"] for rec in prof if rec["kernel"] == dom) / max(dd["launches"], 1)
         out["roofline"]["traffic"] = round(TRAFFIC_PER_SUFFIX[dom] * elems)
-        out["roofline"]["traffic_source"] = ("ncu dram bytes per suffix on the 16 MiB case x suffixes per launch "
-                                             "(profiles/traffic_group_thread_lsd_pass_prose16.md)")
+        out["roofline"]["traffic_source"] = "ncu dram bytes per suffix on the 16 MiB case x suffixes per launch"
     if rank == 0:
         kind, threads, cpu_v, reps = time_cpu(T[: 16 * MIB], r, budget_s=12.0)
         out["cpu_baseline"] = {"value": round(cpu_v, 2), "unit": "MiB/s", "cores": threads, "kind": kind,
