@@ -337,3 +337,79 @@ uint64_t kgbwt_estimate_bytes(int32_t kind, const int32_t *n, const int32_t *r, 
 }
 
 }  // extern "C"
+
+// ---- libcubwt's entry points (include/kgbwt_cubwt.h): a storage is one worker
+#include "kgbwt_cubwt.h"
+
+namespace kgb {
+struct CubwtStorage {
+    unsigned magic = 0x6B637762u;
+    std::mutex mu;
+    Worker w;
+};
+static CubwtStorage *cubwt_of(void *p) {
+    CubwtStorage *s = static_cast<CubwtStorage *>(p);
+    return s && s->magic == 0x6B637762u ? s : nullptr;
+}
+static int64_t cubwt_code(int rc) {
+    return rc == 0 ? KGBWT_CUBWT_NO_ERROR
+           : rc == -1 ? KGBWT_CUBWT_BAD_PARAMETER
+           : rc == -2 ? KGBWT_CUBWT_NOT_ENOUGH_MEMORY
+                      : KGBWT_CUBWT_GPU_ERROR;
+}
+}  // namespace kgb
+
+extern "C" {
+
+int64_t libcubwt_allocate_device_storage(void **device_storage, int64_t max_length) {
+    if (!device_storage || max_length < 0 || max_length > ((int64_t)1 << 30)) return KGBWT_CUBWT_BAD_PARAMETER;
+    CubwtStorage *s = new (std::nothrow) CubwtStorage();
+    if (!s) return KGBWT_CUBWT_NOT_ENOUGH_MEMORY;
+    *device_storage = s;  // the device workspace grows on the first call that needs it
+    return KGBWT_CUBWT_NO_ERROR;
+}
+
+int64_t libcubwt_free_device_storage(void *device_storage) {
+    CubwtStorage *s = cubwt_of(device_storage);
+    if (!s) return KGBWT_CUBWT_BAD_PARAMETER;
+    s->magic = 0;
+    delete s;
+    return KGBWT_CUBWT_NO_ERROR;
+}
+
+int64_t libcubwt_bwt_aux(void *device_storage, const uint8_t *T, uint8_t *L, int64_t n, int64_t r, uint32_t *I) {
+    CubwtStorage *s = cubwt_of(device_storage);
+    if (!s || !T || !L || !I || n < 2 || n > ((int64_t)1 << 30) || r < 2 || r > n || bad_r((int32_t)r))
+        return KGBWT_CUBWT_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lock(s->mu);
+    kgbwt_fwd_job j = {T, L, (int32_t)n, (int32_t)r, reinterpret_cast<int32_t *>(I), 0};
+    const int rc = run_fwd_jobs(s->w, &j, 1, 0);
+    return cubwt_code(rc ? rc : j.rc);
+}
+
+int64_t libcubwt_bwt(void *device_storage, const uint8_t *T, uint8_t *L, int64_t n) {
+    CubwtStorage *s = cubwt_of(device_storage);
+    if (!s || !T || !L || n < 2 || n > ((int64_t)1 << 30)) return KGBWT_CUBWT_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lock(s->mu);
+    // the smallest power of two >= n as the sampling interval: only the primary index is sampled
+    int32_t r = 2;
+    while ((int64_t)r < n) r <<= 1;
+    int32_t idx = 0;
+    kgbwt_fwd_job j = {T, L, (int32_t)n, r, &idx, 0};
+    const int rc = run_fwd_jobs(s->w, &j, 1, 0);
+    const int code = rc ? rc : j.rc;
+    return code ? cubwt_code(code) : (int64_t)idx;
+}
+
+int64_t libcubwt_unbwt(void *device_storage, const uint8_t *T, uint8_t *U, int64_t n, const int32_t *freq, int32_t i) {
+    (void)freq;
+    CubwtStorage *s = cubwt_of(device_storage);
+    if (!s || !T || !U || n < 2 || n > ((int64_t)1 << 30) || i < 1 || i > n) return KGBWT_CUBWT_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lock(s->mu);
+    kgbwt_inv_job j = {T, U, (int32_t)n, (int32_t)n, &i, 0};
+    const int rc = run_inv_jobs(s->w, &j, 1, 0);
+    const int code = j.rc ? j.rc : rc;
+    return code == -1 ? KGBWT_CUBWT_GPU_ERROR : cubwt_code(code);  // -1 here: not a valid BWT
+}
+
+}  // extern "C"

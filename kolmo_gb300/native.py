@@ -128,6 +128,16 @@ def lib():
     L.kgbwt_tuning_load.restype = _I32
     L.kgbwt_tuning_lookup.argtypes = [ctypes.c_uint64, _P]
     L.kgbwt_tuning_lookup.restype = _I32
+    L.libcubwt_allocate_device_storage.argtypes = [_P, ctypes.c_int64]
+    L.libcubwt_allocate_device_storage.restype = ctypes.c_int64
+    L.libcubwt_free_device_storage.argtypes = [_P]
+    L.libcubwt_free_device_storage.restype = ctypes.c_int64
+    L.libcubwt_bwt_aux.argtypes = [_P, _P, _P, ctypes.c_int64, ctypes.c_int64, _P]
+    L.libcubwt_bwt_aux.restype = ctypes.c_int64
+    L.libcubwt_bwt.argtypes = [_P, _P, _P, ctypes.c_int64]
+    L.libcubwt_bwt.restype = ctypes.c_int64
+    L.libcubwt_unbwt.argtypes = [_P, _P, _P, ctypes.c_int64, _P, _I32]
+    L.libcubwt_unbwt.restype = ctypes.c_int64
     L.kgbwt_last_error.restype = ctypes.c_char_p
     L.kgbwt_version.restype = _I32
     _lib = L
@@ -147,4 +157,6 @@ EXPORTS = (
     "kgbwt_unbwt_noalloc", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
     "kgbwt_server_cancel", "kgbwt_server_stats_read", "kgbwt_server_inject_oom", "kgbwt_server_plan",
     "kgbwt_estimate_bytes", "kgbwt_engine_last_config", "kgbwt_tuning_load", "kgbwt_tuning_lookup",
+    "libcubwt_allocate_device_storage", "libcubwt_free_device_storage", "libcubwt_bwt_aux", "libcubwt_bwt",
+    "libcubwt_unbwt",
 )

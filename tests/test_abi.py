@@ -1,4 +1,4 @@
-"""The C-ABI library (no GPU needed): it loads, exports every function include/kgbwt.h declares, and applies the
+"""The C-ABI library (no GPU needed): it loads, exports every function the public headers declare, and applies the
 reference's argument checks before touching the device (src/algo/sais/sais.c:12029-12038, 12057-12068)."""
 import ctypes
 import os
@@ -13,9 +13,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _header_functions():
-    src = open(os.path.join(ROOT, "include", "kgbwt.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(k(?:olmo|gbwt)_\w+)\s*\(", src)))
+    """Every function the public headers (include/kgbwt.h, include/kgbwt_cubwt.h) declare."""
+    names = set()
+    for h in ("kgbwt.h", "kgbwt_cubwt.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b((?:kolmo|kgbwt|libcubwt)_\w+)\s*\(", src))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
@@ -116,3 +120,19 @@ def test_codec18_sampling_rule():
 def test_python_mirror_checks_arguments(lib):
     assert codec.bwt_aux(np.zeros(10, np.uint8), 3)[0] == -1
     assert codec.unbwt(np.zeros(10, np.uint8), 0)[0] == -1
+
+
+def test_cubwt_argument_checks_need_no_device(lib):
+    """libcubwt's entry points refuse bad arguments before touching the device."""
+    st = ctypes.c_void_p()
+    assert lib.libcubwt_allocate_device_storage(ctypes.byref(st), -1) < 0
+    assert lib.libcubwt_allocate_device_storage(ctypes.byref(st), 1 << 20) == 0 and st.value
+    T = np.zeros(64, np.uint8)
+    L = np.zeros(64, np.uint8)
+    I = np.zeros(8, np.uint32)
+    assert lib.libcubwt_bwt_aux(st, T.ctypes.data, L.ctypes.data, 1, 2, I.ctypes.data) < 0      # n < 2
+    assert lib.libcubwt_bwt_aux(st, T.ctypes.data, L.ctypes.data, 64, 3, I.ctypes.data) < 0     # r not 2^k
+    assert lib.libcubwt_bwt_aux(st, T.ctypes.data, L.ctypes.data, 64, 128, I.ctypes.data) < 0   # r > n
+    assert lib.libcubwt_bwt_aux(None, T.ctypes.data, L.ctypes.data, 64, 8, I.ctypes.data) < 0   # no storage
+    assert lib.libcubwt_unbwt(st, T.ctypes.data, L.ctypes.data, 64, None, 0) < 0                # i out of range
+    assert lib.libcubwt_free_device_storage(st) == 0
