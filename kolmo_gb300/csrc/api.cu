@@ -61,6 +61,7 @@ void Worker::release() {
     new (&eng.fwd) FwdEngine();
     eng.inv.~InvEngine();
     new (&eng.inv) InvEngine();
+    stage_L.release();
     stage_I.release();
 }
 Worker::~Worker() {
@@ -78,6 +79,14 @@ static Context &ctx() {
 }
 
 bool bad_r(int32_t r) { return r < 2 || (r & (r - 1)) != 0; }
+
+// Host memory the device can copy into directly (cudaMallocHost / cudaHostRegister): true when the runtime reports a
+// host (page-locked) or managed allocation at p.
+static bool page_locked(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged;
+}
 
 // KGBWT_PLAIN=1 in the environment makes the drop-in and batch calls use the plain path (debugging aid).
 static uint32_t env_flags() {
@@ -117,8 +126,17 @@ int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) 
     if (cudaMemsetAsync(E.text() + E.total(), 0, 64, s) != cudaSuccess)
         return fail(record_cuda_error(cudaGetLastError(), "cudaMemsetAsync", __FILE__, __LINE__));
     if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
-    // sampled indexes first (small), then each block's L column straight into the caller's U, without its sentinel
-    // row (two device-to-host copies per block once the primary index is known)
+    // sampled indexes first (small); then each block's L column without its sentinel row: straight into the
+    // caller's U when every U is page-locked (two device-to-host copies per block), else through one copy into pinned
+    // staging and host copies (device-to-host copies into pageable memory are staged by the driver, block by block)
+    bool direct = true;
+    for (size_t k = 0; k < dev.size() && direct; k++) direct = page_locked(jobs[dev[k]].U);
+    if (!direct) {
+        const size_t lbytes = E.total() + dev.size();
+        if ((rc = C.stage_L.need(lbytes))) return fail(rc);
+        if (cudaMemcpyAsync(C.stage_L.p, E.lcol(), lbytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(L)", __FILE__, __LINE__));
+    }
     if ((rc = C.stage_I.need((size_t)E.samples() * 4))) return fail(rc);
     if (cudaMemcpyAsync(C.stage_I.p, E.samples_dev(), (size_t)E.samples() * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(samples)", __FILE__, __LINE__));
@@ -131,7 +149,15 @@ int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) 
         return fail(-2);
     }
     const u32 *I = reinterpret_cast<const u32 *>(C.stage_I.p);
-    for (size_t k = 0; k < dev.size(); k++) {
+    for (size_t k = 0; k < dev.size() && !direct; k++) {
+        kgbwt_fwd_job &j = jobs[dev[k]];
+        const u8 *L = C.stage_L.p + E.offsets()[k] + k;
+        const u32 p0 = I[E.iouts()[k]];
+        if (p0 < 1 || p0 > (u32)j.n) return fail(-2);
+        memcpy(j.U, L, p0);
+        memcpy(j.U + p0, L + p0 + 1, (size_t)j.n - p0);
+    }
+    for (size_t k = 0; k < dev.size() && direct; k++) {
         kgbwt_fwd_job &j = jobs[dev[k]];
         const u8 *L = E.lcol() + E.offsets()[k] + k;
         const u32 p0 = I[E.iouts()[k]];
@@ -184,6 +210,14 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
         if (cudaMemcpyAsync(E.input() + E.offsets()[k], jobs[dev[k]].T, n[k], cudaMemcpyHostToDevice, s) != cudaSuccess)
             return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(bwt)", __FILE__, __LINE__));
     if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
+    // the decoded texts: straight into the callers' buffers when all are page-locked, else through pinned staging
+    bool direct = true;
+    for (size_t k = 0; k < dev.size() && direct; k++) direct = page_locked(jobs[dev[k]].U);
+    if (!direct) {
+        if ((rc = C.stage_L.need(E.total()))) return fail(rc);
+        if (cudaMemcpyAsync(C.stage_L.p, E.output(), E.total(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
+    }
     std::vector<int> st;
     if ((rc = E.fetch_status(s, st))) return fail(rc);
     int first = 0;
@@ -194,7 +228,10 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
             if (!first) { first = -1; record_error("inverse BWT: not a valid BWT string for its primary index"); }
             continue;
         }
-        // the decoded text straight into the caller's buffer
+        if (!direct) {
+            memcpy(j.U, C.stage_L.p + E.offsets()[k], (size_t)j.n);
+            continue;
+        }
         if (cudaMemcpyAsync(j.U, E.output() + E.offsets()[k], (size_t)j.n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
             return fail(record_cuda_error(cudaGetLastError(), "cudaMemcpyAsync(text)", __FILE__, __LINE__));
     }

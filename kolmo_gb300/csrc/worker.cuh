@@ -32,7 +32,7 @@ struct Pinned {
 struct Worker {
     kgbwt_engine eng;
     cudaStream_t stream = nullptr;
-    Pinned stage_I;  // sampled indexes (results go straight from the device into the caller's buffers)
+    Pinned stage_L, stage_I;  // results for pageable destinations; sampled indexes
     int init();                   // creates the stream on first use
     u64 device_bytes() const { return eng.fwd.workspace_bytes() + eng.inv.workspace_bytes(); }
     void release();               // frees both workspaces and the staging (the stream stays)
