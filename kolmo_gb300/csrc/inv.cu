@@ -36,7 +36,7 @@ constexpr u32 ITILE = 4096;
 constexpr u32 MARK = 64;
 constexpr u32 CAPC = 256;
 constexpr u32 ENDC = 0xFFFFFFFFu;
-constexpr u32 CHUNK = 2048;  // start chains per walk work item
+constexpr u32 CHUNK = 1024;  // start chains per walk work item
 constexpr int KSLOT = 4;     // chains walked at once by one thread
 constexpr u32 CHUNKT = 16;   // tiles per chunk of the psi build
 
