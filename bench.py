@@ -232,7 +232,8 @@ def run_ours(args, world, rank, local):
     ns = n_samples(n, r)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
-    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0)
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0,
+               args.lsd_bytes)
     dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
     dT[:n] = torch.from_numpy(T).to(dev)
     dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
@@ -294,7 +295,7 @@ def run_ours(args, world, rank, local):
                 "fwd_ms": round(sum(tf) / len(tf), 3), "inv_ms": round(sum(ti) / len(ti), 3),
                 "block_bytes": n, "skip_extras": True,
                 "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path,
-                        args.lsd_round0]}
+                        args.lsd_round0, args.lsd_bytes]}
 
     # profiled pass (plain path, CUDA events around every launch on stream s)
     eng.profile(True)
@@ -410,7 +411,8 @@ def run_batch(args, world, rank, local):
     flush = torch.empty(256 * MIB, dtype=torch.uint8, device=dev)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
-    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0)
+    eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0,
+               args.lsd_bytes)
     fblocks = [(off, int(t.size), r, io) for t, off, r, io in zip(texts, offs, rs, iouts)]
 
     def to_u(b_list, I):
@@ -720,6 +722,7 @@ def main():
     ap.add_argument("--small-group", type=int, default=-1)
     ap.add_argument("--warp-path", type=int, default=-1)
     ap.add_argument("--lsd-round0", type=int, default=-1)
+    ap.add_argument("--lsd-bytes", type=int, default=-1, help="prefix bytes of the LSD round 0 (8 or 16)")
     ap.add_argument("--profile-out", default="", help="write the per-launch profile of the profiled step here")
     ap.add_argument("--plain", action="store_true",
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")

@@ -89,19 +89,21 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
  * KGBWT_OPT_SMALL_GROUP (0..1024, default 64): tiles whose groups are all at most this long are sorted by counting
  *   inside each group instead of radix passes (0: always radix).
  * KGBWT_OPT_WARP_PATH (0/1, default 1): tiles whose groups are all at most 32 long go to the warp-level kernel.
- * KGBWT_OPT_LSD_ROUND0 (0/1, default 1): the first round (all suffixes by their 8-byte prefix) is one LSD radix
- *   sort of the whole batch; 0: bucket passes and tile kernels as in the later rounds. */
+ * KGBWT_OPT_LSD_ROUND0 (0/1, default 1): the first round (all suffixes by their prefix) is one LSD radix sort of the
+ *   whole batch; 0: bucket passes and tile kernels over 8-byte prefixes as in the later rounds.
+ * KGBWT_OPT_LSD_BYTES (8 or 16, default 16): prefix bytes that LSD round sorts (16 replaces the first rank round). */
 #define KGBWT_OPT_SMALL_GROUP 1
 #define KGBWT_OPT_WARP_PATH 2
 #define KGBWT_OPT_LSD_ROUND0 3
+#define KGBWT_OPT_LSD_BYTES 4
 int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value);
 /* The configuration the engine's last forward call ran with: tile_cap, tile_ctas, msd_ctas, small_group, warp_path,
- * lsd_round0 (cfg[0..5]). Fields the caller set with kgbwt_engine_config / kgbwt_engine_option are used as set; the
+ * lsd_round0, lsd_bytes (cfg[0..6]). Fields the caller set with kgbwt_engine_config / kgbwt_engine_option are used as set; the
  * others come from the tuning table for the call's batch size when one is loaded, else the defaults. */
 int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg);
 /* Tuning table (no counterpart in the reference): configurations by batch size, a JSON file written by
  * kolmo_gb300/autotune.py ({"buckets": [{"max_bytes": ..., "tile_ctas": ..., "msd_ctas": ..., "small_group": ...,
- * "warp_path": ..., "lsd_round0": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes, else the
+ * "warp_path": ..., "lsd_round0": ..., "lsd_bytes": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes, else the
  * last). Loaded on first use from $KGBWT_TUNING ("off": none), else from tuning_gb300.json in the package directory.
  * kgbwt_tuning_load replaces it (NULL: no table) and returns the number of buckets or -1; kgbwt_tuning_lookup writes
  * the configuration a batch of n bytes would get (as kgbwt_engine_last_config) and returns 1 when it came from the

@@ -5,9 +5,9 @@ tuning_gb300.json beside this package). Results never depend on the configuratio
     python -m kolmo_gb300.autotune --out kolmo_gb300/tuning_gb300.json [--reps 3] [--quick]
 
 Tuned per bucket: CTAs per SM of the block tile kernel (tile_ctas) and of the bucket passes (msd_ctas), the
-counting-sort threshold of the tile kernel (small_group), the warp-level tile path (warp_path) and the round-0 path
-(lsd_round0: one LSD radix sort of all suffixes, or bucket passes + tiles). The tile capacity changes the workspace
-layout and is left at its default.
+counting-sort threshold of the tile kernel (small_group), the warp-level tile path (warp_path), the round-0 path
+(lsd_round0: one LSD radix sort of all suffixes, or bucket passes + tiles) and the prefix it sorts (lsd_bytes: 16,
+which spares the first rank round, or 8). The tile capacity changes the workspace layout and is left at its default.
 """
 from __future__ import annotations
 
@@ -37,6 +37,7 @@ BUCKETS = [
 
 CANDIDATES = {
     "lsd_round0": (1, 0),
+    "lsd_bytes": (16, 8),
     "msd_ctas": (8, 4),
     "tile_ctas": (2, 1),
     "small_group": (64, 0),
@@ -71,7 +72,8 @@ def _time_config(texts, cfg, reps):
     dL = torch.zeros(o + len(texts) + 64, dtype=torch.uint8, device="cuda")
     dI = torch.zeros(k, dtype=torch.int32, device="cuda")
     eng = codec.Engine()
-    eng.config(0, cfg["tile_ctas"], cfg["msd_ctas"], cfg["small_group"], cfg["warp_path"], cfg["lsd_round0"])
+    eng.config(0, cfg["tile_ctas"], cfg["msd_ctas"], cfg["small_group"], cfg["warp_path"], cfg["lsd_round0"],
+               cfg["lsd_bytes"])
     s = torch.cuda.Stream()
     times = []
     ref = None
@@ -96,6 +98,8 @@ def tune(reps: int = 3, quick: bool = False, log=print):
 
     keys = list(CANDIDATES)
     grid = [dict(zip(keys, vals)) for vals in itertools.product(*(CANDIDATES[k] for k in keys))]
+    # the prefix width only matters on the LSD round 0
+    grid = [g for g in grid if g["lsd_round0"] or g["lsd_bytes"] == CANDIDATES["lsd_bytes"][0]]
     if quick:
         grid = grid[:4]
     default = {k: v[0] for k, v in CANDIDATES.items()}

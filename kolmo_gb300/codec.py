@@ -104,16 +104,16 @@ class Engine:
             self.config(tile_cap, tile_ctas, msd_ctas)
 
     def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1,
-               warp_path: int = -1, lsd_round0: int = -1):
+               warp_path: int = -1, lsd_round0: int = -1, lsd_bytes: int = -1):
         L = native.lib()
         rc = L.kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
         for opt, val in ((native.OPT_SMALL_GROUP, small_group), (native.OPT_WARP_PATH, warp_path),
-                         (native.OPT_LSD_ROUND0, lsd_round0)):
+                         (native.OPT_LSD_ROUND0, lsd_round0), (native.OPT_LSD_BYTES, lsd_bytes)):
             if rc == 0 and val >= 0:
                 rc = L.kgbwt_engine_option(self.h, opt, val)
         if rc:
             raise ValueError(f"bad engine config {tile_cap} {tile_ctas} {msd_ctas} {small_group} {warp_path} "
-                             f"{lsd_round0}")
+                             f"{lsd_round0} {lsd_bytes}")
 
     def close(self):
         if self.h:
@@ -170,7 +170,7 @@ class Engine:
 
     def last_config(self) -> dict:
         """The configuration the last forward call ran with (caller settings over the tuning table)."""
-        c = np.zeros(6, np.int32)
+        c = np.zeros(7, np.int32)
         native.lib().kgbwt_engine_last_config(self.h, c.ctypes.data)
         return dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
 
@@ -178,7 +178,7 @@ class Engine:
         return int(native.lib().kgbwt_engine_workspace_bytes(self.h))
 
 
-CONFIG_FIELDS = ("tile_cap", "tile_ctas", "msd_ctas", "small_group", "warp_path", "lsd_round0")
+CONFIG_FIELDS = ("tile_cap", "tile_ctas", "msd_ctas", "small_group", "warp_path", "lsd_round0", "lsd_bytes")
 
 
 def tuning_load(path) -> int:
@@ -188,7 +188,7 @@ def tuning_load(path) -> int:
 
 def tuning_lookup(n: int):
     """(from_table, config) that a batch of n bytes would run with."""
-    c = np.zeros(6, np.int32)
+    c = np.zeros(7, np.int32)
     t = int(native.lib().kgbwt_tuning_lookup(n, c.ctypes.data))
     return t == 1, dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
 

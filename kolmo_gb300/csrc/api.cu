@@ -24,7 +24,7 @@ const char *kernel_name(int k) {
         "tile_sort_rank", "tile_sort_rank_keyed", "control", "samples",
         "tile_warp_prefix", "tile_warp_prefix_keyed", "tile_warp_rank", "tile_warp_rank_keyed",
         "lsd_begin", "lsd_key0", "lsd_hist", "lsd_pass", "seg_count", "seg_scan", "seg_emit1", "seg_emit2",
-        "group_thread", "group_warp", "mkeys",
+        "group_thread", "group_warp", "mkeys", "lsd_rekey",
         "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
@@ -242,7 +242,7 @@ int run_inv_jobs(Worker &C, kgbwt_inv_job *jobs, int32_t count, uint32_t flags) 
 
 // ---- tuning table: configurations by batch size, written by kolmo_gb300/autotune.py as JSON
 // {"buckets": [{"max_bytes": B, "tile_ctas": ..., "msd_ctas": ..., "small_group": ..., "warp_path": ...,
-// "lsd_round0": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes (else the last).
+// "lsd_round0": ..., "lsd_bytes": ...}, ...]}; a batch of n bytes takes the first bucket with n <= max_bytes (else the last).
 struct TuneBucket {
     u64 max_bytes;
     FwdConfig c;
@@ -302,6 +302,7 @@ static int parse_tuning(const char *text, std::vector<TuneBucket> &out) {
             else if (key == "small_group") { if (v < 0 || v > 1024) return -1; b.c.small_group = (int)v; }
             else if (key == "warp_path") { if (v != 0 && v != 1) return -1; b.c.warp_path = (int)v; }
             else if (key == "lsd_round0") { if (v != 0 && v != 1) return -1; b.c.lsd_round0 = (int)v; }
+            else if (key == "lsd_bytes") { if (v != 8 && v != 16) return -1; b.c.lsd_bytes = (int)v; }
         }
         if (!have_max) return -1;
         out.push_back(b);
@@ -446,6 +447,11 @@ int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
             e->fwd.ucfg.lsd_round0 = value;
             e->fwd.cfg_explicit |= CFG_LSD_ROUND0;
             return 0;
+        case KGBWT_OPT_LSD_BYTES:
+            if (value != 8 && value != 16) return -1;
+            e->fwd.ucfg.lsd_bytes = value;
+            e->fwd.cfg_explicit |= CFG_LSD_BYTES;
+            return 0;
         default:
             return -1;
     }
@@ -563,7 +569,7 @@ int32_t kgbwt_tuning_lookup(uint64_t n, int32_t *cfg) {
     FwdConfig c;
     const bool t = tuned_config(n, &c);
     cfg[0] = c.tile_cap; cfg[1] = c.tile_ctas; cfg[2] = c.msd_ctas; cfg[3] = c.small_group; cfg[4] = c.warp_path;
-    cfg[5] = c.lsd_round0;
+    cfg[5] = c.lsd_round0; cfg[6] = c.lsd_bytes;
     return t ? 1 : 0;
 }
 
@@ -572,7 +578,7 @@ int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg) {
     std::lock_guard<std::mutex> lock(e->mu);
     const FwdConfig &c = e->fwd.cfg;
     cfg[0] = c.tile_cap; cfg[1] = c.tile_ctas; cfg[2] = c.msd_ctas; cfg[3] = c.small_group; cfg[4] = c.warp_path;
-    cfg[5] = c.lsd_round0;
+    cfg[5] = c.lsd_round0; cfg[6] = c.lsd_bytes;
     return 0;
 }
 

@@ -62,6 +62,7 @@ struct FwdArgs {
     u32 B;
     u32 smax;
     u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
+    u32 lsd_bytes;    // prefix bytes of the LSD round 0 (8 or 16)
     u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
@@ -69,6 +70,7 @@ struct FwdArgs {
     u32 *lkh[2], *lkl[2];  // round 0: the 8-byte keys carried with the ids (high / low halves)
     u64 *lstat;
     u32 *lhist, *ltile, *segagg;
+    u32 *lbase;  // round 0: per block and digit slot, the pass's first position of every digit
     u32 spin_limit;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segk, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
@@ -1495,7 +1497,7 @@ __global__ void k_ctl_round_end(FwdArgs a) {
     c->cnt[L_R0 + (rp ^ 1)] = 0;
     c->rpar = rp ^ 1;
     c->round += 1;
-    c->h = c->round == 1 ? 8 : c->h * 2;
+    c->h = c->round == 1 ? c->h0 : c->h * 2;
     c->pass = 0;
     u32 cont = active > 0;
     if (cont && c->round > c->maxrounds) { c->err |= 1; cont = 0; }
@@ -1593,15 +1595,16 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_dest, nseg_large * 256);
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
-    const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
+    const u64 ltiles = n / LSD_TILE + bcap + 2, stiles = n / SEG_TILE + 2;
     // the round-0 radix buffers (ids and block indexes, ping-pong) alias the bucket-pass work lists K0 / K1, and the
     // key halves alias the large list L0 and the keyed small list KS: round 0 on the LSD path uses none of those lists,
     // and in the rank rounds the medium-key scratch (lval[0]) is written after the round's bucket passes and read
     // before the next round's
     add((void **)&d_lstat, ltiles * 256 * 8);
     add((void **)&d_segbits, n / 8 + 64);
-    add((void **)&d_lhist, NSLOT * 256 * 4);
-    add((void **)&d_ltile, 64);
+    add((void **)&d_lhist, (size_t)bcap * 256 * 4);  // byte histogram of every block
+    add((void **)&d_lbase, (size_t)bcap * NSLOT * 256 * 4);
+    add((void **)&d_ltile, NSLOT * 4);
     add((void **)&d_segagg, stiles * 8 * 4);
     add((void **)&d_ctl, sizeof(Ctl));
 }
@@ -1635,7 +1638,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     const u64 nseg_med = n / (GTINY + 1) + bcap + 8;
     const u64 nseg_s = n / (GMED + 1) + bcap + 8;
     const u64 ntm_small = n / smax + 8, ntm_large = n / TSM + 8;
-    const u64 ltiles = n / LSD_TILE + 2, stiles = n / SEG_TILE + 2;
+    const u64 ltiles = n / LSD_TILE + bcap + 2, stiles = n / SEG_TILE + 2;
     size_t total = 0;
     for (auto &it : items) total += it.bytes;
     cudaError_t e = cudaMalloc(&pool, total);
@@ -1680,9 +1683,10 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     for (int q = 0; q < 2; q++) { a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
     a.lkh[0] = lists[L_L0].eid; a.lkl[0] = lists[L_L0].ekey; a.lkh[1] = lists[L_KS].eid; a.lkl[1] = lists[L_KS].ekey;
     a.segbits = d_segbits;
-    a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg;
+    a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg; a.lbase = d_lbase;
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
+    a.lsd_bytes = (u32)cfg.lsd_bytes;
     a.warp_path = (u32)cfg.warp_path;
     a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segk = cap_segk; a.cap_segl = cap_segl; a.cap_segt = cap_segt;
     a.cap_segm = cap_segm;
@@ -1745,6 +1749,7 @@ void FwdEngine::resolve_config() {
     if (!(cfg_explicit & CFG_SMALL_GROUP)) cfg.small_group = t.small_group;
     if (!(cfg_explicit & CFG_WARP_PATH)) cfg.warp_path = t.warp_path;
     if (!(cfg_explicit & CFG_LSD_ROUND0)) cfg.lsd_round0 = t.lsd_round0;
+    if (!(cfg_explicit & CFG_LSD_BYTES)) cfg.lsd_bytes = t.lsd_bytes;
 }
 
 static int ceil_log2(u64 x) { int k = 0; while ((1ull << k) < x) k++; return k; }
@@ -1755,15 +1760,16 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     // block table, round-0 lists and their tile maps are laid out on the host (B entries, small)
     const u32 smax = (u32)cfg.tile_cap / 2;
     std::vector<BlockInfo> bi(B);
-    u32 soff_b = 0;
+    u32 soff_b = 0, lt_b = 0;
     std::vector<u32> lstart(B);
     std::vector<u8> large(B);
     std::vector<Seg> seg_s, seg_l;
     std::vector<u32> tm_s, tm_l, big_s;
     u64 es = 0, el = 0;
     for (u32 b = 0; b < B; b++) {
-        bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b], soff_b, 0};
+        bi[b] = BlockInfo{h_off[b], h_n[b], h_r[b], h_iout[b], soff_b, lt_b};
         soff_b += h_n[b];
+        lt_b += (h_n[b] + LSD_TILE - 1) / LSD_TILE;
         large[b] = h_n[b] > smax;
         Seg g;
         g.len = h_n[b]; g.head = 0; g.bd = b;
@@ -1788,6 +1794,8 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     c.cnt[L_L0] = ((u64)seg_l.size() << 32) | el;
     c.maxrounds = (u32)ceil_log2(maxn) + 3;
     c.seq = ++call_seq;
+    c.h0 = lsd_enabled() ? (u32)cfg.lsd_bytes : 8u;
+    c.lsd_tiles = lt_b;
     KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
     const size_t ntm = cap_tms;
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemsetAsync(lists[l].tbig, 0xFF, ntm * 4, s));
@@ -1830,7 +1838,7 @@ static FwdArgs make_args(Ctl *ctl, const u8 *T, const BlockInfo *blk, u32 *const
     return a;
 }
 
-static size_t lsd_smem(bool hi) { return hi ? sizeof(LsdSmem<true>) : sizeof(LsdSmem<false>); }
+static size_t lsd_smem() { return sizeof(LsdSmem); }
 template <bool PREFIX, int TILE>
 static int tile_smem() { return (int)sizeof(TileSmem<TILE, typename TileTraits<PREFIX, TILE>::KeyT>); }
 template <bool PREFIX, int TILE>
@@ -1879,8 +1887,7 @@ static int set_tile_attrs(int tile) {
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, false, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
         KGB_CHECK(cudaFuncSetAttribute(k_tile_warp<false, true, 8192>, cudaFuncAttributeMaxDynamicSharedMemorySize, warp_smem<false, 8192>()));
     }
-    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem(false)));
-    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem(true)));
+    KGB_CHECK(cudaFuncSetAttribute(k_lsd_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsd_smem()));
     g_attr_done[idx] = true;
     return 0;
 }
@@ -1967,20 +1974,24 @@ static int report_err(u32 bits) {
 static cudaError_t enq_lsd_keys(Launcher &L, const FwdArgs &a) {
     cudaError_t e;
     L.tag(K_LSD_BEGIN, 0);
-    if ((e = L.go(k_lsd_begin, 1, 256, 0, a))) return e;
+    if ((e = L.go(k_lsd_begin, L.grid_msd, 256, 0, a))) return e;
     L.tag(K_LSD_KEY0, 0);
     if ((e = L.go(k_lsd_key0, L.grid_msd, TPB, 0, a))) return e;
     L.tag(K_LSD_HIST, 0);
-    return L.go(k_lsd_hist0, 1, 256, 0, a);
+    return L.go(k_lsd_hist0, std::min<int>((int)a.B, L.grid_msd), TPB, 0, a);
 }
 static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u32 m_tag) {
     cudaError_t e;
     for (int slot = 0; slot < NSLOT; slot++) {
+        if (slot == 8 && a.lsd_bytes == 16) {  // the passes over bytes 7..0 carry the prefix's first word
+            if (L.prof) L.prof->pass = -1;
+            L.tag(K_LSD_REKEY, m_tag);
+            if ((e = L.go(k_lsd_rekey, L.grid_msd, TPB, 0, a))) return e;
+        }
         if (!((slots >> slot) & 1)) continue;
         L.tag(K_LSD_PASS, m_tag);
         if (L.prof) L.prof->pass = slot;
-        if ((e = a.B > 1 ? L.go(k_lsd_pass<true>, L.grid_lsd, TPB, lsd_smem(true), a, slot)
-                         : L.go(k_lsd_pass<false>, L.grid_lsd, TPB, lsd_smem(false), a, slot)))
+        if ((e = L.go(k_lsd_pass, L.grid_lsd, TPB, lsd_smem(), a, slot)))
             return e;
     }
     if (L.prof) L.prof->pass = -1;
@@ -1994,14 +2005,7 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
     return L.go(k_seg_emit2, L.grid_msd, TPB, 0, a);
 }
 
-static u32 host_active_slots(const Ctl &c) {
-    const u64 vl = c.vary_lo ^ c.and_lo;
-    const u32 vh = c.vary_hi ^ c.and_hi;
-    u32 m = 0;
-    for (int q = 0; q < 8; q++) if ((vl >> (8 * q)) & 0xFF) m |= 1u << q;
-    for (int q = 0; q < 4; q++) if ((vh >> (8 * q)) & 0xFF) m |= 1u << (8 + q);
-    return m;
-}
+static u32 host_active_slots(const Ctl &c) { return c.lsd_act; }
 
 int FwdEngine::run_plain(cudaStream_t s) {
     const u32 smax = (u32)cfg.tile_cap / 2;
@@ -2240,7 +2244,7 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     grid_tile = sm_count * (cfg.tile_cap == 4096 ? std::min(std::max(cfg.tile_ctas, 1), 2) : 1);
     grid_tile_prefix = sm_count * (cfg.tile_cap == 4096 ? 2 : 1);
     grid_warp = sm_count * (cfg.tile_cap == 4096 ? 4 : 2);
-    grid_lsd = (int)((N + LSD_TILE - 1) / LSD_TILE);
+    grid_lsd = (int)((N + LSD_TILE - 1) / LSD_TILE + B);  // at least the batch's sort tiles (one partial per block)
     grid_msd = sm_count * cfg.msd_ctas;
     grid_scan = sm_count * 4;
     // the host-side round-0 layout borrows the cursor/dest rows; they are rewritten by every bucket scan

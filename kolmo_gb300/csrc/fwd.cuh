@@ -13,7 +13,7 @@ struct FwdArgs;
 struct BlockInfo {
     u32 off, n, r, iout;
     u32 soff;  // first position of the block in the dense order of all suffixes of the batch (prefix sum of n)
-    u32 pad;
+    u32 lt0;   // first round-0 sort tile of the block (tiles never straddle blocks)
 };
 
 // A segment of an element list: `len` consecutive elements starting at `start` that form one group (equal sort
@@ -53,12 +53,11 @@ struct Ctl {
     u32 done;
     u32 err;
     u32 maxrounds;
-    u32 pad;
+    u32 lsd_tiles;    // round-0 sort tiles of the batch
     u64 tile_elems[2];  // elements sorted so far by the block-level and the warp-level tile kernels (statistics)
     // round 0 as an LSD radix sort
-    u64 vary_lo;        // OR / AND of the sort keys (which key bytes vary)
-    u64 and_lo;
-    u32 vary_hi, and_hi;
+    u32 lsd_act;        // bit s: digit slot s varies (a pass runs for it)
+    u32 h0;             // characters round 0 sorts (the first rank round's h)
     u32 m;              // suffixes sorted
     u32 seq;            // call sequence number (tags the look-back words of the radix passes)
     u32 p_alloc;        // slots taken so far in the tiny-group id array (shared by both parities, never reused)
@@ -70,10 +69,13 @@ struct FwdConfig {
     int msd_ctas = 8;     // persistent CTAs per SM for the bucket passes
     int small_group = 64; // tiles whose groups are all at most this long skip the radix passes (counting sort)
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
-    int lsd_round0 = 1;   // round 0 (8-byte prefixes) as one LSD radix sort of all suffixes; 0: bucket passes + tiles
+    int lsd_round0 = 1;   // round 0 as one LSD radix sort of all suffixes; 0: bucket passes + tiles over 8-byte prefixes
+    int lsd_bytes = 16;   // prefix bytes the LSD round 0 sorts (8 or 16)
 };
 // Fields of FwdConfig a caller set explicitly (they override the tuning table).
-enum : u32 { CFG_TILE_CTAS = 1, CFG_MSD_CTAS = 2, CFG_SMALL_GROUP = 4, CFG_WARP_PATH = 8, CFG_LSD_ROUND0 = 16 };
+enum : u32 {
+    CFG_TILE_CTAS = 1, CFG_MSD_CTAS = 2, CFG_SMALL_GROUP = 4, CFG_WARP_PATH = 8, CFG_LSD_ROUND0 = 16, CFG_LSD_BYTES = 32
+};
 // The tuning table's configuration for a batch of n text bytes: fills the fields the table sets (tile_ctas,
 // msd_ctas, small_group, warp_path, lsd_round0) and returns true, or returns false when no table is loaded.
 bool tuned_config(u64 n, FwdConfig *out);
@@ -161,6 +163,7 @@ class FwdEngine {
     // LSD path
     u32 *d_lval[2] = {nullptr, nullptr}, *d_lhi[2] = {nullptr, nullptr};
     u64 *d_lstat = nullptr;
+    u32 *d_lbase = nullptr;
     u32 *d_lhist = nullptr, *d_ltile = nullptr, *d_segagg = nullptr, *d_segbits = nullptr;
     u64 lsd_tiles_cap = 0, seg_tiles_cap = 0;
     u8 *d_dest = nullptr;
@@ -185,7 +188,8 @@ class FwdEngine {
             return N == o.N && Ncap == o.Ncap && B == o.B && T == o.T && L == o.L && I == o.I && SA == o.SA &&
                    cfg.tile_cap == o.cfg.tile_cap && cfg.tile_ctas == o.cfg.tile_ctas &&
                    cfg.msd_ctas == o.cfg.msd_ctas && cfg.small_group == o.cfg.small_group &&
-                   cfg.warp_path == o.cfg.warp_path && cfg.lsd_round0 == o.cfg.lsd_round0 && lsd == o.lsd;
+                   cfg.warp_path == o.cfg.warp_path && cfg.lsd_round0 == o.cfg.lsd_round0 &&
+                   cfg.lsd_bytes == o.cfg.lsd_bytes && lsd == o.lsd;
         }
     };
     GraphKey graph_key{};

@@ -1,174 +1,218 @@
-// Round 0 of the forward sort as one LSD radix sort: every suffix of the batch is sorted by (block, zero-padded
-// 8-byte prefix) with one pass per varying key byte (single-pass scatter with decoupled look-back), then a
-// segmentation turns the sorted order into ranks, finished suffixes and the rank rounds' groups (the small-group list
-// for the tile kernels, the large-group list for the bucket passes). The passes move (key, id) items, the 8-byte key
-// as two 32-bit halves (and the block index when the batch has several blocks): a pass takes its digit from the key
-// it carries, and the segmentation compares neighbouring keys without touching the text. Included by fwd.cu inside
-// namespace kgb, after the kernels it shares (FwdArgs, resolve, tile-map writers).
+// Round 0 of the forward sort as one LSD radix sort: the suffixes of each block of the batch are sorted by their
+// zero-padded W-byte prefix, W = 16 (or 8), with one pass per varying key byte (single-pass scatter with decoupled
+// look-back), then a segmentation turns the sorted order into ranks, finished suffixes and the rank rounds' groups
+// (tiny, medium, small and large lists). The sort tiles never straddle two blocks: every block's suffixes keep their
+// own range of the dense order (the block's soff onward), a pass takes each tile's digit bases from its own block's
+// counts and looks back only over the block's earlier tiles, so the block index is neither carried nor sorted. The
+// passes move (key, id) items with one 8-byte key word carried as two 32-bit halves: the passes over bytes 15..8
+// carry the second word, a re-key kernel then loads the first word for the passes over bytes 7..0; a pass takes its
+// digit from the word it carries. The segmentation compares the carried first word and, for W = 16, the second word
+// read from the text. Sorting 16 bytes here replaces the first rank round (which would take the groups from 8 to 16
+// bytes) with eight passes over all suffixes. Included by fwd.cu inside namespace kgb, after the kernels it shares
+// (FwdArgs, resolve, tile-map writers).
 #pragma once
 // (included inside namespace kgb)
 
 constexpr int LSD_IPT = 16, LSD_TILE = TPB * LSD_IPT;  // elements per sort tile
-constexpr int NSLOT = 12;                              // digit slots: key bytes 0..7, then block-index bytes 0..3
+// digit slots: slot s sorts prefix byte 15 - s (0..7: the second key word, 8..15: the first)
+constexpr int NSLOT = 16;
+static_assert(NSLOT <= 32, "the look-back epoch holds the slot in 5 bits");
 constexpr int SEG_IPT = 16, SEG_TILE = TPB * SEG_IPT;  // positions per segmentation tile (SEG_IPT <= 32)
-// look-back words: epoch (32 bits: call sequence, digit slot) | flag (2 bits) | value (30 bits); a word of another
+// look-back words: epoch (32 bits: call sequence << 5 | digit slot) | flag (2 bits) | value (30 bits); a word of another
 // epoch (an earlier slot or call) counts as not yet published
 constexpr u64 ST_AGG = 1ull << 30, ST_PRE = 2ull << 30, ST_VAL = (1ull << 30) - 1;
 constexpr u64 ST_EPOCH = 0xFFFFFFFF00000000ull;
 constexpr int LB_WIN = 8;  // look-back window (predecessor words read per step)
 
-__device__ __forceinline__ u32 active_slots(const Ctl *c) {  // bit s: key byte s varies
-    const u64 vl = c->vary_lo ^ c->and_lo;
-    const u32 vh = c->vary_hi ^ c->and_hi;
-    u32 m = 0;
-#pragma unroll
-    for (int s = 0; s < 8; s++) m |= ((vl >> (8 * s)) & 0xFF) ? 1u << s : 0u;
-#pragma unroll
-    for (int s = 0; s < 4; s++) m |= ((vh >> (8 * s)) & 0xFF) ? 1u << (8 + s) : 0u;
-    return m;
-}
-__device__ __forceinline__ bool lsd_has_hi(const FwdArgs &a) { return a.B > 1; }
+__device__ __forceinline__ u32 active_slots(const Ctl *c) { return c->lsd_act; }  // bit s: slot s varies
 
-// The zero-padded 8-byte prefix of suffix id (block ending at end) as a big-endian word.
-__device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u32 id, u64 end) {
-    u64 k = load_be64(T, id);
-    const u64 rem = end - id;
+// The zero-padded 8-byte text word at position q of a block ending at end, as a big-endian word (0 past the end).
+__device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u64 q, u64 end) {
+    if (q >= end) return 0;
+    u64 k = load_be64(T, q);
+    const u64 rem = end - q;
     if (rem < 8) k &= ~0ull << (8 * (8 - rem));
     return k;
 }
 
-// Start (256 threads): clear the text byte histogram, the tile counters and the resolved count.
+// The block of sort tile t: the last block whose first tile (lt0) is <= t (blocks in batch order, lt0 ascending).
+__device__ __forceinline__ u32 blk_of_tile(const FwdArgs &a, u32 t) {
+    u32 lo = 0, hi = a.B - 1;
+    while (lo < hi) {
+        const u32 mid = (lo + hi + 1) >> 1;
+        if (__ldg(&a.blk[mid].lt0) <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+// The block holding dense position p, searched within blocks [lo, hi]: the last block whose soff is <= p.
+__device__ __forceinline__ u32 blk_of_pos(const FwdArgs &a, u32 p, u32 lo, u32 hi) {
+    while (lo < hi) {
+        const u32 mid = (lo + hi + 1) >> 1;
+        if (__ldg(&a.blk[mid].soff) <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+// A sort tile: its block, first dense position and element count.
+struct LsdTile {
+    u32 b, base, cnt;
+};
+__device__ __forceinline__ LsdTile lsd_tile(const FwdArgs &a, u32 t) {
+    LsdTile r;
+    r.b = blk_of_tile(a, t);
+    const BlockInfo bi = a.blk[r.b];
+    const u32 k = (t - bi.lt0) * (u32)LSD_TILE;
+    r.base = bi.soff + k;
+    r.cnt = min((u32)LSD_TILE, bi.n - k);
+    return r;
+}
+
+// Start: clear the blocks' byte histograms, the tile counters, the active mask and the resolved count.
 __global__ void k_lsd_begin(FwdArgs a) {
     Ctl *c = a.ctl;
-    for (int i = threadIdx.x; i < NSLOT * 256; i += blockDim.x) a.lhist[i] = 0;
-    if (threadIdx.x < NSLOT) a.ltile[threadIdx.x] = 0;
-    if (threadIdx.x == 0) c->cnt[L_R0 + c->rpar] = 0;
+    const u64 nh = (u64)a.B * 256;
+    for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += (u64)gridDim.x * blockDim.x) a.lhist[i] = 0;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x < NSLOT) a.ltile[threadIdx.x] = 0;
+        if (threadIdx.x == 0) {
+            c->cnt[L_R0 + c->rpar] = 0;
+            c->lsd_act = 0;
+            c->m = a.blk[a.B - 1].soff + a.blk[a.B - 1].n;
+        }
+    }
 }
 
-// Suffix ids and their 8-byte keys in the dense order of the batch (block index beside them when the batch has
-// several blocks), and the byte histogram of the whole text (row 0 of the histogram table), from which every pass's
-// digit counts follow.
+// Suffix ids in the dense order of the batch with the key word the first passes need (the second word of the
+// prefix for W = 16, else the first), and each block's byte histogram, from which every pass's digit counts follow.
+// CTA c takes a contiguous run of sort tiles and adds its shared histogram into a block's row when the run leaves it.
 __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
     __shared__ u32 hs[256];
-    const bool hi = lsd_has_hi(a);
-    const u64 stride = (u64)gridDim.x * blockDim.x;
+    const u32 woff = a.lsd_bytes == 16 ? 8u : 0u;
+    const u32 nt = a.ctl->lsd_tiles;
+    const u32 per = (nt + gridDim.x - 1) / gridDim.x;
+    const u32 t0 = blockIdx.x * per, t1 = min(nt, t0 + per);
     hs[threadIdx.x] = 0;
     __syncthreads();
-    for (u32 b = 0; b < a.B; b++) {
-        const BlockInfo bi = a.blk[b];
+    u32 cur = ~0u;  // block whose counts hs holds
+    for (u32 t = t0; t < t1; t++) {
+        const LsdTile tl = lsd_tile(a, t);
+        if (tl.b != cur) {
+            if (cur != ~0u) {
+                __syncthreads();
+                const u32 v = hs[threadIdx.x];
+                if (v) atomicAdd(&a.lhist[(u64)cur * 256 + threadIdx.x], v);
+                hs[threadIdx.x] = 0;
+                __syncthreads();
+            }
+            cur = tl.b;
+        }
+        const BlockInfo bi = a.blk[tl.b];
+        const u64 end = (u64)bi.off + bi.n;
         // row 0 of the L column (the sentinel rotation) holds the block's last byte
-        if (blockIdx.x == 0 && threadIdx.x == 0) a.L[(u64)bi.off + b] = a.T[(u64)bi.off + bi.n - 1];
-        for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < bi.n; j += stride) {
-            const u32 id = bi.off + (u32)j;
-            const u64 x = (u64)bi.soff + j;
+        if (t == bi.lt0 && threadIdx.x == 0) a.L[(u64)bi.off + tl.b] = a.T[end - 1];
+        const u32 id0 = bi.off + (tl.base - bi.soff);
+        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) {
+            const u32 id = id0 + j;
+            const u64 x = (u64)tl.base + j;
             __stcs(a.lval[0] + x, id);
-            if (hi) __stcs(a.lhi[0] + x, b);
-            const u64 k = lsd_key(a.T, id, (u64)bi.off + bi.n);
+            const u64 k = lsd_key(a.T, (u64)id + woff, end);
             __stcs(a.lkh[0] + x, (u32)(k >> 32));
             __stcs(a.lkl[0] + x, (u32)k);
-            atomicAdd(&hs[(u32)(k >> 56)], 1u);
+            atomicAdd(&hs[__ldg(a.T + id)], 1u);
         }
     }
     __syncthreads();
-    if (hs[threadIdx.x]) atomicAdd(&a.lhist[threadIdx.x], hs[threadIdx.x]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->m = a.B ? a.blk[a.B - 1].soff + a.blk[a.B - 1].n : 0;
+    if (cur != ~0u && hs[threadIdx.x]) atomicAdd(&a.lhist[(u64)cur * 256 + threadIdx.x], hs[threadIdx.x]);
 }
 
-// Digit counts of every pass (one CTA of 256 threads, thread = digit value). Suffix i of a block of n bytes has key
-// byte d = T[i + d] when i + d < n, else 0, so the counts of key byte d are the block's byte counts minus those of
-// its first min(d, n) bytes, plus min(d, n) zeros; block-index digits count each block's n. A slot whose counts sit
-// in one digit is constant: the vary words mark the others, which the passes run.
-__global__ void k_lsd_hist0(FwdArgs a) {
-    __shared__ u32 pre[8][256];  // pre[d][x]: bytes x among the first d bytes of every block (d = 1..7)
-    __shared__ u32 zeros[8];
-    __shared__ u32 hib[4][256];
-    __shared__ u32 flag[NSLOT];
+// Digit bases of every pass and the active slots (256 threads per CTA, thread = digit value, CTAs over blocks).
+// Suffix i of a block of n bytes has key byte d = T[i + d] when i + d < n, else 0, so the counts of key byte d are
+// the block's byte counts minus those of its first min(d, n) bytes, plus min(d, n) zeros; their exclusive scan plus
+// the block's soff gives the pass's first position of every digit (lbase row (block, slot), slot = 15 - d). A slot
+// runs when its key byte takes two or more values within some block (slots 8..15 only for W = 8).
+__global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
+    __shared__ u32 wm[8];
+    __shared__ u32 ws[TPB / 32 + 1];
     const u32 x = threadIdx.x;
-    for (int d = 0; d < 8; d++) pre[d][x] = 0;
-    for (int q = 0; q < 4; q++) hib[q][x] = 0;
-    if (x < 8) zeros[x] = 0;
-    if (x < NSLOT) flag[x] = 0;
-    __syncthreads();
-    for (u32 b = x; b < a.B; b += blockDim.x) {
+    const int first = a.lsd_bytes == 16 ? 0 : 8;
+    for (u32 b = blockIdx.x; b < a.B; b += gridDim.x) {
         const BlockInfo bi = a.blk[b];
-        for (u32 d = 1; d < 8; d++) {
-            if (d <= bi.n) atomicAdd(&pre[d][a.T[(u64)bi.off + d - 1]], 1u);
-            atomicAdd(&zeros[d], d < bi.n ? d : bi.n);  // min(d, n) zero digits per block
+        const u32 h = a.lhist[(u64)b * 256 + x];
+        u32 pre = 0, mask = 0;  // pre: bytes x among the block's first d bytes
+        for (int slot = 15; slot >= first; slot--) {
+            const u32 d = 15 - slot;
+            if (d >= 1 && d <= bi.n) pre += __ldg(a.T + (u64)bi.off + d - 1) == x;
+            const u32 v = h - pre + (x == 0 ? min(d, bi.n) : 0u);
+            if (v != 0 && v != bi.n) mask |= 1u << slot;
+            a.lbase[((u64)b * NSLOT + slot) * 256 + x] = bi.soff + block_excl_sum<TPB>(v, ws, nullptr);
         }
-        if (a.B > 1)
-            for (int q = 0; q < 4; q++) atomicAdd(&hib[q][(b >> (8 * q)) & 0xFF], bi.n);
-    }
-    __syncthreads();
-    // pre[d] holds the bytes at offset d - 1 only: accumulate to the first d bytes
-    for (int d = 2; d < 8; d++) pre[d][x] += pre[d - 1][x];
-    const u32 m = a.ctl->m;
-    const u32 h0 = a.lhist[x];  // byte counts of the whole text
-    for (int slot = 0; slot < 8; slot++) {
-        const u32 d = 7 - slot;
-        const u32 v = d ? h0 - pre[d][x] + (x == 0 ? zeros[d] : 0u) : h0;
-        a.lhist[slot * 256 + x] = v;
-        if (v != 0 && v != m) flag[slot] = 1;  // at least two digits occur
-    }
-    if (a.B > 1)
-        for (int q = 0; q < 4; q++) {
-            const u32 v = hib[q][x];
-            a.lhist[(8 + q) * 256 + x] = v;
-            if (v != 0 && v != m) flag[8 + q] = 1;
+        for (int o = 16; o; o >>= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
+        if ((x & 31) == 0) wm[x >> 5] = mask;
+        __syncthreads();
+        if (x == 0) {
+            u32 m = 0;
+            for (int w = 0; w < 8; w++) m |= wm[w];
+            if (m & ~a.ctl->lsd_act) atomicOr(&a.ctl->lsd_act, m);
         }
-    __syncthreads();
-    if (x == 0) {
-        Ctl *c = a.ctl;
-        u64 vl = 0;
-        u32 vh = 0;
-        for (int q = 0; q < 8; q++) if (flag[q]) vl |= 0xFFull << (8 * q);
-        for (int q = 0; q < 4; q++) if (flag[8 + q]) vh |= 0xFFu << (8 * q);
-        c->vary_lo = vl; c->and_lo = 0; c->vary_hi = vh; c->and_hi = 0;
+        __syncthreads();
     }
 }
 
-template <bool HI>
+// Between the passes over bytes 15..8 and those over bytes 7..0 (W = 16): replace every carried key word with the
+// first word of its suffix's prefix, read from the text, in the order the first passes left (tile by tile: a tile's
+// positions belong to one block).
+__global__ void __launch_bounds__(TPB) k_lsd_rekey(FwdArgs a) {
+    const Ctl *c = a.ctl;
+    const u32 par = __popc(active_slots(c) & 0xFFu) & 1;
+    const u32 nt = c->lsd_tiles;
+    for (u32 t = blockIdx.x; t < nt; t += gridDim.x) {
+        const LsdTile tl = lsd_tile(a, t);
+        const u64 end = blk_end(a, tl.b);
+        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) {
+            const u64 x = (u64)tl.base + j;
+            const u32 id = __ldcs(a.lval[par] + x);
+            const u64 k = lsd_key(a.T, id, end);
+            __stcs(a.lkh[par] + x, (u32)(k >> 32));
+            __stcs(a.lkl[par] + x, (u32)k);
+        }
+    }
+}
+
 struct LsdSmem {
     u32 val[LSD_TILE];
     u32 kh[LSD_TILE], kl[LSD_TILE];
-    u32 hi[HI ? LSD_TILE : 1];
     u8 dg[LSD_TILE];
     u16 wcnt[TPB / 32][256];
     u32 gbase[256];
-    u32 dbase[256];
     u32 ws[TPB / 32 + 1];
     u32 tile;
 };
 
-// One LSD pass over digit `slot` (skipped when that key byte is the same in every key): rank the tile's suffixes by
-// digit, publish the tile's digit counts, look back over earlier tiles for the global offsets (bounded spin), stage
-// the tile in shared memory in digit order and write it out in runs.
-template <bool HI>
-__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
+// One LSD pass over digit `slot` (skipped when that key byte is constant within every block): rank the tile's
+// suffixes by digit, publish the tile's digit counts, look back over the block's earlier tiles for the offsets
+// (bounded spin), stage the tile in shared memory in digit order and write it out in runs.
+__global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    LsdSmem<HI> &S = *reinterpret_cast<LsdSmem<HI> *>(smem_raw);
+    LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
     const Ctl *c = a.ctl;
     const u32 act = active_slots(c);
     if (!((act >> slot) & 1)) return;
     const u32 par = __popc(act & ((1u << slot) - 1)) & 1;
-    const u32 m = c->m;
-    const u32 ntiles = (m + LSD_TILE - 1) / LSD_TILE;
-    const u64 epoch = (u64)((c->seq << 4) | (u32)slot) << 32;
+    const u32 ntiles = c->lsd_tiles;
+    const u64 epoch = (u64)((c->seq << 5) | (u32)slot) << 32;
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
-    // digit bases of the pass: exclusive scan of the slot's counts
-    {
-        const u32 hcount = a.lhist[slot * 256 + tid];
-        S.dbase[tid] = block_excl_sum<TPB>(hcount, S.ws, nullptr);
-    }
     for (int i = tid; i < (TPB / 32) * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
     __syncthreads();
     const u32 tile = S.tile;
     if (tile >= ntiles) return;
-    const u32 base = tile * LSD_TILE;
-    const u32 cnt = min((u32)LSD_TILE, m - base);
-    const u32 *vin = a.lval[par], *hin = a.lhi[par], *khin = a.lkh[par], *klin = a.lkl[par];
+    const LsdTile tl = lsd_tile(a, tile);
+    const u32 base = tl.base, cnt = tl.cnt;
+    const bool head = tile == __ldg(&a.blk[tl.b].lt0);  // the block's first tile: its counts are the inclusive prefix
+    // this pass's first position of digit tid in the block
+    const u32 dbase = __ldg(a.lbase + ((u64)tl.b * NSLOT + slot) * 256 + tid);
+    const u32 *vin = a.lval[par], *khin = a.lkh[par], *klin = a.lkl[par];
     // rk[j]: rank in the warp's digit bucket (bits 0..15) | digit, 0x100 past the end (bits 16..24)
-    u32 v[LSD_IPT], hh[LSD_IPT], rk[LSD_IPT], kh[LSD_IPT], kl[LSD_IPT];
+    u32 v[LSD_IPT], rk[LSD_IPT], kh[LSD_IPT], kl[LSD_IPT];
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
@@ -176,14 +220,11 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         v[j] = ok ? __ldcs(vin + base + x) : 0u;
         kh[j] = ok ? __ldcs(khin + base + x) : 0u;
         kl[j] = ok ? __ldcs(klin + base + x) : 0u;
-        hh[j] = ok && HI ? __ldcs(hin + base + x) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        u32 d;
-        if (slot >= 8) d = (hh[j] >> (8 * (slot - 8))) & 0xFFu;
-        else d = ((slot < 4 ? kl[j] : kh[j]) >> (8 * (slot & 3))) & 0xFFu;
+        const u32 d = (((slot & 7) < 4 ? kl[j] : kh[j]) >> (8 * (slot & 3))) & 0xFFu;
         rk[j] = (x < cnt ? d : 0x100u) << 16;
     }
 #pragma unroll
@@ -202,7 +243,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 #pragma unroll
     for (int w = 0; w < TPB / 32; w++) tot += S.wcnt[w][tid];
     u64 *st = a.lstat + (u64)tile * 256 + tid;
-    if (tile == 0) atomicExch((unsigned long long *)st, epoch | ST_PRE | tot);
+    if (head) atomicExch((unsigned long long *)st, epoch | ST_PRE | tot);
     else atomicExch((unsigned long long *)st, epoch | ST_AGG | tot);
     const u32 dstart = block_excl_sum<TPB>(tot, S.ws, nullptr);
     {
@@ -220,14 +261,14 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
             S.val[p] = v[j];
             S.kh[p] = kh[j];
             S.kl[p] = kl[j];
-            if (HI) S.hi[p] = hh[j];
             S.dg[p] = (u8)d;
         }
     }
     u32 excl = 0;
-    if (tile > 0) {
+    if (!head) {
         // windowed look-back: read LB_WIN predecessors' words at once, add aggregates in order up to the first
-        // inclusive prefix; a word not yet published ends the window and the walk resumes there
+        // inclusive prefix (at the latest the block's first tile); a word not yet published ends the window and the
+        // walk resumes there
         long j = (long)tile - 1;
         u32 spins = 0;
         while (true) {
@@ -258,16 +299,16 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         }
         atomicExch((unsigned long long *)st, epoch | ST_PRE | (u64)(excl + tot));
     }
-    S.gbase[tid] = S.dbase[tid] + excl - dstart;
+    S.gbase[tid] = dbase + excl - dstart;
     __syncthreads();
-    u32 *vout = a.lval[par ^ 1], *hout = a.lhi[par ^ 1], *khout = a.lkh[par ^ 1], *klout = a.lkl[par ^ 1];
+    u32 *vout = a.lval[par ^ 1], *khout = a.lkh[par ^ 1], *klout = a.lkl[par ^ 1];
     for (u32 i = tid; i < cnt; i += TPB) {
         const u32 dst = S.gbase[S.dg[i]] + i;
-        if (KGB_OK(dst < m, &a.ctl->err, E_LIST)) {
+        if (KGB_OK(dst < base - (tile - __ldg(&a.blk[tl.b].lt0)) * LSD_TILE + __ldg(&a.blk[tl.b].n), &a.ctl->err,
+                   E_LIST)) {
             __stcs(vout + dst, S.val[i]);
             __stcs(khout + dst, S.kh[i]);
             __stcs(klout + dst, S.kl[i]);
-            if (HI) __stcs(hout + dst, S.hi[i]);
         }
     }
 }
@@ -280,53 +321,64 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 __device__ __forceinline__ u32 lsd_final_par(const Ctl *c) { return __popc(active_slots(c)) & 1; }
 
 struct SegBufs {
-    const u32 *val, *hi;
+    const u32 *val;
     u32 *bits;          // start bitmask
-    u32 *gbase, *gidx;  // per group start: list slot base, list index | GRP_LARGE (free value / block buffers)
-    bool has_hi;
+    u32 *gbase, *gidx;  // per group start: list slot base, list index | GRP_LARGE (free value buffers)
     u32 m;
 };
 __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
     const Ctl *c = a.ctl;
     const u32 par = lsd_final_par(c);
     SegBufs v;
-    v.val = a.lval[par]; v.hi = a.lhi[par];
+    v.val = a.lval[par];
     v.bits = a.segbits;
     v.gbase = a.lval[par ^ 1];
     v.gidx = a.lhi[par ^ 1];
-    v.has_hi = lsd_has_hi(a);
     v.m = c->m;
     return v;
 }
 constexpr u32 GRP_LARGE = 0x80000000u, GRP_TINY = 0x40000000u, GRP_MED = 0x20000000u;
 constexpr u32 SEG_WORDS = SEG_IPT;  // mask words per warp chunk
 
-// Per tile: start bits and the tile's last group start (position 0 always starts a group).
+// The blocks a warp's chunk of SEG_IPT * 32 positions from cb spans: [lo, hi] (the same for every lane).
+__device__ __forceinline__ uint2 seg_chunk_blocks(const FwdArgs &a, u32 cb, u32 m) {
+    const u32 lo = blk_of_pos(a, cb, 0, a.B - 1);
+    const u32 hi = blk_of_pos(a, min(cb + SEG_IPT * 32, m) - 1, lo, a.B - 1);
+    return make_uint2(lo, hi);
+}
+
+// Per tile: start bits and the tile's last group start (position 0 always starts a group, and so does every block's
+// first position).
 __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     __shared__ u32 ws[TPB / 32];
     const SegBufs v = seg_bufs(a);
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 lane = lane_id(), warp = warp_id();
+    const bool w16 = a.lsd_bytes == 16;
+    const u32 fp = lsd_final_par(a.ctl);
+    const u32 *KH = a.lkh[fp], *KL = a.lkl[fp];
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
+        const uint2 br = cb < v.m ? seg_chunk_blocks(a, cb, v.m) : make_uint2(0u, 0u);
         u32 last = 0;
 #pragma unroll 4
         for (int j = 0; j < SEG_IPT; j++) {
             const u32 p = cb + j * 32 + lane;
             const bool ok = p < v.m;
-            const u32 fp = lsd_final_par(a.ctl);
-            const u32 *KH = a.lkh[fp], *KL = a.lkl[fp];
-            u32 h = ok && v.has_hi ? v.hi[p] : 0u;
+            const u32 b = ok ? (br.x == br.y ? br.x : blk_of_pos(a, p, br.x, br.y)) : 0u;
+            const BlockInfo bi = a.blk[b];
+            const u64 end = (u64)bi.off + bi.n;
             u64 k = ok ? ((u64)KH[p] << 32) | KL[p] : 0ull;
-            u64 kp = __shfl_up_sync(0xffffffffu, k, 1);
-            u32 hp = __shfl_up_sync(0xffffffffu, h, 1);
-            if (lane == 0 && ok && p > 0) {
-                hp = v.has_hi ? v.hi[p - 1] : 0u;
+            // the second 8-byte word of the prefix (W = 16), from the text
+            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)v.val[p] + 8, end) : 0ull;
+            u64 kp = __shfl_up_sync(0xffffffffu, k, 1), k2p = __shfl_up_sync(0xffffffffu, k2, 1);
+            if (lane == 0 && ok && p > bi.soff) {  // the neighbour is in the same block
                 kp = ((u64)KH[p - 1] << 32) | KL[p - 1];
+                k2p = w16 ? lsd_key(a.T, (u64)v.val[p - 1] + 8, end) : 0ull;
             }
-            const bool st = ok && (p == 0 || k != kp || h != hp);
-            const u32 b = __ballot_sync(0xffffffffu, st);
-            if (lane == 0 && cb + j * 32 < v.m) v.bits[(cb >> 5) + j] = b;
+            const bool st = ok && (p == bi.soff || k != kp || k2 != k2p);
+            const u32 sb = __ballot_sync(0xffffffffu, st);
+            if (lane == 0 && cb + j * 32 < v.m) v.bits[(cb >> 5) + j] = sb;
             if (st) last = p;
         }
 #pragma unroll
@@ -365,6 +417,7 @@ __global__ void __launch_bounds__(1024) k_seg_scan(FwdArgs a) {
 // first position.
 struct SegChunk {
     u32 cb, word, nextw, carry0;
+    u32 blo, bhi;  // the blocks the chunk spans
 };
 __device__ __forceinline__ SegChunk seg_chunk(const FwdArgs &a, const SegBufs &v, u32 t, u32 *wl) {
     const u32 lane = lane_id(), warp = warp_id();
@@ -384,6 +437,8 @@ __device__ __forceinline__ SegChunk seg_chunk(const FwdArgs &a, const SegBufs &v
     u32 cr = a.segagg[(u64)t * 2 + 1];
     for (u32 w = 0; w < warp; w++) cr = max(cr, wl[w]);
     c.carry0 = cr;
+    const uint2 br = c.cb < v.m ? seg_chunk_blocks(a, c.cb, v.m) : make_uint2(0u, 0u);
+    c.blo = br.x; c.bhi = br.y;
     return c;
 }
 // Position j * 32 + lane of the chunk: start / end flags and the group's first position (carry: running start).
@@ -498,7 +553,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
 #pragma unroll
             for (int q = 0; q < QB; q++) {
                 if (!((live >> q) & 1)) continue;
-                bv[q] = v.has_hi ? __ldg(v.hi + pv[q]) : 0u;
+                bv[q] = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, pv[q], ch.blo, ch.bhi);
                 idv[q] = pv[q] == gfv[q] ? __ldg(v.val + pv[q]) : 0u;  // ids of finished suffixes (groups of one)
             }
 #pragma unroll
@@ -584,7 +639,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
             for (int q = 0; q < QB; q++) {
                 if (!((live >> q) & 1)) continue;
                 idv[q] = __ldg(v.val + pv[q]);
-                bv[q] = v.has_hi ? __ldg(v.hi + pv[q]) : 0u;
+                bv[q] = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, pv[q], ch.blo, ch.bhi);
                 giv[q] = __ldg(v.gidx + gfv[q]);
                 gbv[q] = __ldg(v.gbase + gfv[q]);
             }

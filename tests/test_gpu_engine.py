@@ -87,16 +87,18 @@ def test_engine_configs_give_identical_results():
         assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
 
 
-@pytest.mark.parametrize("lsd_round0", [0, 1])
-def test_round0_paths_on_mixed_batch(lsd_round0):
-    """Round 0 as one LSD radix sort of the batch, or as bucket passes + tiles: both must give the oracle's L column
-    and sampled indexes, on a batch that mixes two-byte blocks (the engine's minimum), runs longer than a tile (large groups spanning
+@pytest.mark.parametrize("lsd_round0,lsd_bytes", [(0, 16), (1, 8), (1, 16)])
+def test_round0_paths_on_mixed_batch(lsd_round0, lsd_bytes):
+    """Round 0 as one LSD radix sort of the batch (over 8- or 16-byte prefixes, sort tiles aligned to the blocks), or
+    as bucket passes + tiles: each must give the oracle's L column and sampled indexes, on a batch that mixes two-byte
+    blocks (the engine's minimum), blocks shorter than the prefix, runs longer than a tile (large groups spanning
     segmentation tiles) and ordinary text."""
     import torch
 
     texts = [np.array([7, 1], np.uint8), np.array([3, 3], np.uint8), np.full(20_000, 97, np.uint8),
              W.periodic(60_000, 11, 7, 1 << 14), W.markov2(90_000, 12), W.test_block(5, 5_000),
-             np.zeros(3_000, np.uint8), W.zipf_prose(150_000, 13)]
+             np.array([5, 0, 5, 0, 5, 0, 5, 0, 5, 0, 5], np.uint8), np.zeros(3_000, np.uint8),
+             W.zipf_prose(150_000, 13), np.array([2, 1, 2], np.uint8)]
     buf, offs = _pack(texts)
     r = 1 << 10
     iouts, k = [], 0
@@ -107,7 +109,7 @@ def test_round0_paths_on_mixed_batch(lsd_round0):
     dL = torch.zeros(buf.size + len(texts), dtype=torch.uint8, device="cuda")
     dI = torch.zeros(k, dtype=torch.int32, device="cuda")
     eng = codec.Engine()
-    eng.config(lsd_round0=lsd_round0)
+    eng.config(lsd_round0=lsd_round0, lsd_bytes=lsd_bytes)
     blocks = [(off, t.size, r, io) for t, off, io in zip(texts, offs, iouts)]
     for _ in range(2):  # the second call reuses the captured graph and the look-back words of the first
         assert eng.fwd(dT, dL, dI, blocks) == 0
@@ -133,7 +135,7 @@ def test_tuning_table_applies_and_explicit_settings_win(tmp_path):
     dT = torch.zeros(n + 64, dtype=torch.uint8, device="cuda")
     dT[:n] = torch.from_numpy(t).cuda()
     table = {"buckets": [{"max_bytes": 1 << 40, "tile_ctas": 1, "msd_ctas": 3, "small_group": 0, "warp_path": 0,
-                          "lsd_round0": 0}]}
+                          "lsd_round0": 0, "lsd_bytes": 8}]}
     p = tmp_path / "tune.json"
     p.write_text(json.dumps(table))
     pkg = os.path.join(os.path.dirname(codec.__file__), "tuning_gb300.json")
@@ -143,13 +145,14 @@ def test_tuning_table_applies_and_explicit_settings_win(tmp_path):
         for explicit in (False, True):
             eng = codec.Engine()
             if explicit:
-                eng.config(0, 2, 8, 64, 1, 1)
+                eng.config(0, 2, 8, 64, 1, 1, 16)
             dL = torch.zeros(n + 1, dtype=torch.uint8, device="cuda")
             dI = torch.zeros(4, dtype=torch.int32, device="cuda")
             assert eng.fwd(dT, dL, dI, [(0, n, 1 << 20, 0)]) == 0 and eng.wait()[0] == 0
             c = eng.last_config()
-            want = (2, 8, 64, 1, 1) if explicit else (1, 3, 0, 0, 0)
-            assert (c["tile_ctas"], c["msd_ctas"], c["small_group"], c["warp_path"], c["lsd_round0"]) == want
+            want = (2, 8, 64, 1, 1, 16) if explicit else (1, 3, 0, 0, 0, 8)
+            assert (c["tile_ctas"], c["msd_ctas"], c["small_group"], c["warp_path"], c["lsd_round0"],
+                    c["lsd_bytes"]) == want
             outs.append((dL.cpu().numpy(), dI.cpu().numpy()))
             eng.close()
         assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])

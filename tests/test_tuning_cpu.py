@@ -48,7 +48,7 @@ def test_no_table_gives_defaults(restore_table):
     assert codec.tuning_load(None) == 0
     hit, c = codec.tuning_lookup(64 << 20)
     assert not hit and c == {"tile_cap": 4096, "tile_ctas": 2, "msd_ctas": 8, "small_group": 64, "warp_path": 1,
-                             "lsd_round0": 1}
+                             "lsd_round0": 1, "lsd_bytes": 16}
 
 
 def test_packaged_table_parses_if_present(restore_table):
