@@ -195,14 +195,14 @@ TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 22.5}
 def algorithmic_bytes(rec: dict) -> float:
     """Algorithmic bytes of one launch (the per-unit figures of the doubling model): a rank round costs 48 B per
     active suffix (read its id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id),
-    round 0 33 B per suffix, the inverse 10 B per byte over its passes (psi build: read L, write psi; walk: read psi,
-    write text)."""
+    a round-0 radix pass 24 B per suffix (read and write its 12 B item: id and one 8-byte key word), the inverse 10 B
+    per byte over its passes (psi build: read L, write psi; walk: read psi, write text)."""
     k, e = rec["kernel"], rec["elems"]
     if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed", "group_thread",
              "group_warp"):
         return 48.0 * e
     if k == "lsd_pass":
-        return 3.0 * e   # round 0 sorts every suffix once: its 24 B (key, id) read+write spread over 8 byte passes
+        return 24.0 * e  # every pass reads and writes each suffix's 12 B item
     if k in ("tile_sort_prefix", "tile_sort_prefix_keyed", "tile_warp_prefix", "tile_warp_prefix_keyed"):
         return 33.0 * e
     if k == "inv_walk":
@@ -331,11 +331,13 @@ def run_ours(args, world, rank, local):
         if rec["kernel"] in ("tile_sort_rank", "tile_warp_rank", "group_thread", "group_warp", "keygen"):
             rr["m"] += rec["elems"]
     round_table = []
+    lc = eng.last_config()
+    h0 = lc["lsd_bytes"] if lc["lsd_round0"] else 8  # prefix bytes round 0 sorts (the first rank round's h)
     for j in sorted(rounds):
         m = rounds[j]["m"] if j > 0 else n
         b = (48.0 if j > 0 else 33.0) * m
         ms = rounds[j]["ms"]
-        round_table.append({"round": j, "h": 0 if j == 0 else 8 << (j - 1), "m": m, "ms": round(ms, 4),
+        round_table.append({"round": j, "h": 0 if j == 0 else h0 << (j - 1), "m": m, "ms": round(ms, 4),
                             "GBs": round(b / (ms / 1e3) / 1e9, 1) if ms > 0 else None})
 
     # e2e through the drop-in C ABI with pinned host buffers
@@ -354,8 +356,8 @@ def run_ours(args, world, rank, local):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "launches_per_step": dd["launches"], "share": round(dd["ms"] / tot_ms, 4),
-                     "bytes_model": "rank round 48 B per active suffix, round 0 33 B per suffix (per launch: "
-                                    "elements of the launch's work list)"},
+                     "bytes_model": "rank round 48 B per active suffix, round-0 radix pass 24 B per suffix (per "
+                                    "launch: elements of the launch's work list)"},
         "kernel_shares": {k: round(v["ms"] / tot_ms, 4) for k, v in sorted(by_kernel.items(), key=lambda x: -x[1]["ms"])},
         "rounds": round_table,
         "gpu_launches": args.steps * (launches_fwd + launches_inv),
@@ -557,8 +559,12 @@ def run_serve(args, world, rank, local):
     arrivals = np.cumsum(gaps) - gaps[0]
     total = sum(int(T.size) for _, T, _ in reqs)
 
+    # one server for the warm-up rounds and the timed round: its workers keep their workspaces resident, as a
+    # long-running server does
+    srv = codec.Server(slots=args.slots, hbm_budget=150 * 10**9)
+
     def serve_once():
-        srv = codec.Server(slots=args.slots, hbm_budget=150 * 10**9)
+        before = srv.stats()
         handles = [None] * count
         t0 = time.perf_counter()
 
@@ -580,6 +586,7 @@ def run_serve(args, world, rank, local):
             lat[i] = us / 1e3
         t_end = time.perf_counter()
         stats = srv.stats()
+        stats = {"batches": stats["batches"] - before["batches"], "hbm_peak": stats["hbm_peak"]}
         # results equal the drop-in calls (spot check every 8th request)
         for i in range(0, count, 8):
             kind, T, r = reqs[i]
@@ -588,13 +595,13 @@ def run_serve(args, world, rank, local):
                 assert np.array_equal(handles[i][1], U) and np.array_equal(handles[i][2], I)
             else:
                 assert np.array_equal(handles[i][1], T)
-        srv.close()
         return lat, t_end - t0, stats
 
     for _ in range(max(args.warmup, 1) if args.warmup else 1):
         serve_once()
     barrier(world)
     lat, wall, stats = serve_once()
+    srv.close()
     value = total / MIB / wall
     # serial per-request plain path: service times alone, then a FIFO single server over the same arrivals
     svc = np.zeros(count)
@@ -620,7 +627,8 @@ def run_serve(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": f"serve: {count} Poisson requests at {args.rate}/s, 30% compress / 70% decompress, "
                                "lognormal sizes (median 256 KiB, sigma 1.5, cap 128 MiB), batch sources",
-                   "slots": args.slots, "hbm_budget": 150 * 10**9, "bytes": total},
+                   "slots": args.slots, "hbm_budget": 150 * 10**9, "bytes": total,
+                   "server": "warm: the warm-up rounds run the same stream on the same server"},
         "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
         "serial_plain": {"value": round(serial_v, 2), "unit": "MiB/s",
                          "p50_ms": round(float(np.percentile(slat, 50)), 3),

@@ -2252,6 +2252,11 @@ int FwdEngine::run(cudaStream_t s, bool use_graph) {
     if (!use_graph) return run_plain(s);
     const GraphKey key{N, Ncap, B, d_T, d_L, d_I, d_SA, cfg, lsd_enabled()};
     if (!gexec || !(key == graph_key)) {
+        if (!(seen_valid && key == seen_key)) {  // first sight of this shape: plain launches, no capture
+            seen_key = key;
+            seen_valid = true;
+            return run_plain(s);
+        }
         // capture on the engine's own stream: the caller's may be the legacy default stream, which cannot capture
         if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
         if (int rc = build_graph(cap_stream)) return rc;

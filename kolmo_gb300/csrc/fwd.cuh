@@ -193,6 +193,10 @@ class FwdEngine {
         }
     };
     GraphKey graph_key{};
+    // the shape of the last call that ran without a graph: a shape runs as plain launches the first time it is seen
+    // and is captured when it comes back (a capture costs more than the plain path saves on one call)
+    GraphKey seen_key{};
+    bool seen_valid = false;
     int sm_count = 0;
     int grid_tile = 0, grid_msd = 0, grid_scan = 0, grid_tile_prefix = 0, grid_warp = 0, grid_lsd = 0;
 };

@@ -545,9 +545,13 @@ int InvEngine::run(cudaStream_t s, bool use_graph) {
     prof_run = !use_graph && prof.on;
     if (!use_graph) return enqueue(s, &stats.launches);
     prof_run = false;
-    const u64 key = ((u64)B << 40) ^ N ^ ((u64)(uintptr_t)d_U << 1) ^ ((u64)(uintptr_t)d_out << 3) ^ (nchunk_all << 17) ^
-                    (nchains << 23) ^ ((u64)njump << 58) ^ ((u64)nchunks << 29) ^ (Ncap << 11);
-    if (!gexec || key != graph_key) {
+    const GraphKey key{N, Ncap, (u64)nchunk_all, (u64)nchains, (u32)B, njump, nchunks, d_U, d_out};
+    if (!gexec || !(key == graph_key)) {
+        if (!(seen_valid && key == seen_key)) {  // first sight of this shape: plain launches, no capture
+            seen_key = key;
+            seen_valid = true;
+            return enqueue(s, &stats.launches);
+        }
         if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
         if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
         if (!cap_stream) KGB_CHECK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));

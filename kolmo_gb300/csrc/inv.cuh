@@ -73,7 +73,19 @@ class InvEngine {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t cap_stream = nullptr;
-    u64 graph_key = 0;
+    // everything a captured graph depends on; a shape runs as plain launches the first time it is seen and is
+    // captured when it comes back
+    struct GraphKey {
+        u64 N, Ncap, nchunk_all, nchains;
+        u32 B, njump, nchunks;
+        const void *U, *out;
+        bool operator==(const GraphKey &o) const {
+            return N == o.N && Ncap == o.Ncap && nchunk_all == o.nchunk_all && nchains == o.nchains && B == o.B &&
+                   njump == o.njump && nchunks == o.nchunks && U == o.U && out == o.out;
+        }
+    };
+    GraphKey graph_key{}, seen_key{};
+    bool seen_valid = false;
     int sm_count = 0;
 };
 

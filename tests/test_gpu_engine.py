@@ -111,9 +111,11 @@ def test_round0_paths_on_mixed_batch(lsd_round0, lsd_bytes):
     eng = codec.Engine()
     eng.config(lsd_round0=lsd_round0, lsd_bytes=lsd_bytes)
     blocks = [(off, t.size, r, io) for t, off, io in zip(texts, offs, iouts)]
-    for _ in range(2):  # the second call reuses the captured graph and the look-back words of the first
+    for it in range(3):  # plain launches (first sight of the shape), then capture, then the cached graph
+        dL.zero_()
         assert eng.fwd(dT, dL, dI, blocks) == 0
         assert eng.wait()[0] == 0
+        assert (eng.stats()["launches"] > 0) == (it == 0), it
         L = dL.cpu().numpy()
         I = dI.cpu().numpy()
         for b, (t, off, io) in enumerate(zip(texts, offs, iouts)):

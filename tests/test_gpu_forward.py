@@ -94,11 +94,13 @@ def test_plain_path_equals_graph_path(golden):
     assert cases
     blocks = [(make_input(c), c["r"]) for c in cases]
     rc1, a = codec.fwd_batch(blocks, plain=True)
-    rc2, b = codec.fwd_batch(blocks, plain=False)
-    assert rc1 == rc2 == 0
-    for c, x, y in zip(cases, a, b):
-        assert np.array_equal(x[1], y[1]) and np.array_equal(x[2], y[2])
-        assert h(x[1]) == c["U"]
+    assert rc1 == 0
+    for _ in range(2):  # a batch shape is captured as a graph the second time the graph path sees it
+        rc2, b = codec.fwd_batch(blocks, plain=False)
+        assert rc2 == 0
+        for c, x, y in zip(cases, a, b):
+            assert np.array_equal(x[1], y[1]) and np.array_equal(x[2], y[2])
+            assert h(x[1]) == c["U"]
 
 
 def test_in_place_T_equals_U():
