@@ -67,7 +67,7 @@ struct FwdArgs {
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
     u32 *lval[2], *lhi[2], *segbits;
-    u32 *lkh[2], *lkl[2];  // round 0: the 8-byte keys carried with the ids (high / low halves)
+    u32 *lkey[2];  // round 0: the 4-byte key groups carried with the ids
     u64 *lstat;
     u32 *lhist, *ltile, *segagg;
     u32 *lbase;  // round 0: per block and digit slot, the pass's first position of every digit
@@ -1596,8 +1596,8 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
     const u64 ltiles = n / LSD_TILE + bcap + 2, stiles = n / SEG_TILE + 2;
-    // the round-0 radix buffers (ids and block indexes, ping-pong) alias the bucket-pass work lists K0 / K1, and the
-    // key halves alias the large list L0 and the keyed small list KS: round 0 on the LSD path uses none of those lists,
+    // the round-0 radix buffers (ids, ping-pong) alias the bucket-pass work lists K0 / K1, and the key groups alias
+    // the large list L0 and the keyed small list KS: round 0 on the LSD path uses none of those lists,
     // and in the rank rounds the medium-key scratch (lval[0]) is written after the round's bucket passes and read
     // before the next round's
     add((void **)&d_lstat, ltiles * 256 * 8);
@@ -1681,7 +1681,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 void FwdEngine::set_caps(FwdArgs &a) const {
     a.orand64 = d_orand64;
     for (int q = 0; q < 2; q++) { a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
-    a.lkh[0] = lists[L_L0].eid; a.lkl[0] = lists[L_L0].ekey; a.lkh[1] = lists[L_KS].eid; a.lkl[1] = lists[L_KS].ekey;
+    a.lkey[0] = lists[L_L0].eid; a.lkey[1] = lists[L_KS].eid;
     a.segbits = d_segbits;
     a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg; a.lbase = d_lbase;
     a.spin_limit = 1u << 22;
@@ -1982,12 +1982,10 @@ static cudaError_t enq_lsd_keys(Launcher &L, const FwdArgs &a) {
 }
 static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u32 m_tag) {
     cudaError_t e;
+    if (L.prof) L.prof->pass = -1;
+    L.tag(K_LSD_IDENT, m_tag);
+    if ((e = L.go(k_lsd_ident, L.grid_msd, TPB, 0, a))) return e;
     for (int slot = 0; slot < NSLOT; slot++) {
-        if (slot == 8 && a.lsd_bytes == 16) {  // the passes over bytes 7..0 carry the prefix's first word
-            if (L.prof) L.prof->pass = -1;
-            L.tag(K_LSD_REKEY, m_tag);
-            if ((e = L.go(k_lsd_rekey, L.grid_msd, TPB, 0, a))) return e;
-        }
         if (!((slots >> slot) & 1)) continue;
         L.tag(K_LSD_PASS, m_tag);
         if (L.prof) L.prof->pass = slot;

@@ -4,17 +4,18 @@
 // (tiny, medium, small and large lists). The sort tiles never straddle two blocks: every block's suffixes keep their
 // own range of the dense order (the block's soff onward), a pass takes each tile's digit bases from its own block's
 // counts and looks back only over the block's earlier tiles, so the block index is neither carried nor sorted. The
-// passes move (key, id) items with one 8-byte key word carried as two 32-bit halves: the passes over bytes 15..8
-// carry the second word, a re-key kernel then loads the first word for the passes over bytes 7..0; a pass takes its
-// digit from the word it carries. The segmentation compares the carried first word and, for W = 16, the second word
-// read from the text. Sorting 16 bytes here replaces the first rank round (which would take the groups from 8 to 16
-// bytes) with eight passes over all suffixes. Included by fwd.cu inside namespace kgb, after the kernels it shares
-// (FwdArgs, resolve, tile-map writers).
+// passes move 8-byte (id, key) items whose key is the 4-byte group of prefix bytes the passes of that group sort:
+// the first pass builds its items from the text (ids still in text order, so the loads coalesce), and the last pass
+// of a group writes the next group's key, gathered from the text (which stays in L2 at these sizes), so each pass
+// reads and writes 16 B per suffix. The segmentation compares the whole W-byte prefixes, read from the text. Sorting
+// 16 bytes here replaces the first rank round (which would take the groups from 8 to 16 bytes) with eight passes over
+// all suffixes. Included by fwd.cu inside namespace kgb, after the kernels it shares (FwdArgs, resolve, tile-map
+// writers).
 #pragma once
 // (included inside namespace kgb)
 
 constexpr int LSD_IPT = 16, LSD_TILE = TPB * LSD_IPT;  // elements per sort tile
-// digit slots: slot s sorts prefix byte 15 - s (0..7: the second key word, 8..15: the first)
+// digit slots: slot s sorts prefix byte 15 - s, carried in key group (15 - s) / 4 (bytes 4g..4g+3, big-endian)
 constexpr int NSLOT = 16;
 static_assert(NSLOT <= 32, "the look-back epoch holds the slot in 5 bits");
 constexpr int SEG_IPT = 16, SEG_TILE = TPB * SEG_IPT;  // positions per segmentation tile (SEG_IPT <= 32)
@@ -34,6 +35,12 @@ __device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u64 q, u64 end)
     if (rem < 8) k &= ~0ull << (8 * (8 - rem));
     return k;
 }
+// Key group g (prefix bytes 4g..4g+3) of the suffix at id, big-endian, zero past the block end.
+__device__ __forceinline__ u32 lsd_group(const u8 *__restrict__ T, u32 id, u32 g, u64 end) {
+    return (u32)(lsd_key(T, (u64)id + 4 * g, end) >> 32);
+}
+// Key group of slot s.
+__device__ __forceinline__ u32 lsd_slot_group(int slot) { return (15u - (u32)slot) >> 2; }
 
 // The block of sort tile t: the last block whose first tile (lt0) is <= t (blocks in batch order, lt0 ascending).
 __device__ __forceinline__ u32 blk_of_tile(const FwdArgs &a, u32 t) {
@@ -81,12 +88,10 @@ __global__ void k_lsd_begin(FwdArgs a) {
     }
 }
 
-// Suffix ids in the dense order of the batch with the key word the first passes need (the second word of the
-// prefix for W = 16, else the first), and each block's byte histogram, from which every pass's digit counts follow.
-// CTA c takes a contiguous run of sort tiles and adds its shared histogram into a block's row when the run leaves it.
+// Each block's byte histogram, from which every pass's digit counts follow, and row 0 of its L column. CTA c takes a
+// contiguous run of sort tiles and adds its shared histogram into a block's row when the run leaves it.
 __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
     __shared__ u32 hs[256];
-    const u32 woff = a.lsd_bytes == 16 ? 8u : 0u;
     const u32 nt = a.ctl->lsd_tiles;
     const u32 per = (nt + gridDim.x - 1) / gridDim.x;
     const u32 t0 = blockIdx.x * per, t1 = min(nt, t0 + per);
@@ -110,15 +115,7 @@ __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
         // row 0 of the L column (the sentinel rotation) holds the block's last byte
         if (t == bi.lt0 && threadIdx.x == 0) a.L[(u64)bi.off + tl.b] = a.T[end - 1];
         const u32 id0 = bi.off + (tl.base - bi.soff);
-        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) {
-            const u32 id = id0 + j;
-            const u64 x = (u64)tl.base + j;
-            __stcs(a.lval[0] + x, id);
-            const u64 k = lsd_key(a.T, (u64)id + woff, end);
-            __stcs(a.lkh[0] + x, (u32)(k >> 32));
-            __stcs(a.lkl[0] + x, (u32)k);
-            atomicAdd(&hs[__ldg(a.T + id)], 1u);
-        }
+        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) atomicAdd(&hs[__ldg(a.T + id0 + j)], 1u);
     }
     __syncthreads();
     if (cur != ~0u && hs[threadIdx.x]) atomicAdd(&a.lhist[(u64)cur * 256 + threadIdx.x], hs[threadIdx.x]);
@@ -157,29 +154,22 @@ __global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
     }
 }
 
-// Between the passes over bytes 15..8 and those over bytes 7..0 (W = 16): replace every carried key word with the
-// first word of its suffix's prefix, read from the text, in the order the first passes left (tile by tile: a tile's
-// positions belong to one block).
-__global__ void __launch_bounds__(TPB) k_lsd_rekey(FwdArgs a) {
+// When no key byte varies within any block, no pass runs: the sorted order is the text order (ids written here for
+// the segmentation). Otherwise returns at once.
+__global__ void __launch_bounds__(TPB) k_lsd_ident(FwdArgs a) {
     const Ctl *c = a.ctl;
-    const u32 par = __popc(active_slots(c) & 0xFFu) & 1;
+    if (active_slots(c)) return;
     const u32 nt = c->lsd_tiles;
     for (u32 t = blockIdx.x; t < nt; t += gridDim.x) {
         const LsdTile tl = lsd_tile(a, t);
-        const u64 end = blk_end(a, tl.b);
-        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) {
-            const u64 x = (u64)tl.base + j;
-            const u32 id = __ldcs(a.lval[par] + x);
-            const u64 k = lsd_key(a.T, id, end);
-            __stcs(a.lkh[par] + x, (u32)(k >> 32));
-            __stcs(a.lkl[par] + x, (u32)k);
-        }
+        const u32 id0 = a.blk[tl.b].off + (tl.base - a.blk[tl.b].soff);
+        for (u32 j = threadIdx.x; j < tl.cnt; j += TPB) __stcs(a.lval[0] + tl.base + j, id0 + j);
     }
 }
 
 struct LsdSmem {
     u32 val[LSD_TILE];
-    u32 kh[LSD_TILE], kl[LSD_TILE];
+    u32 key[LSD_TILE];
     u8 dg[LSD_TILE];
     u16 wcnt[TPB / 32][256];
     u32 gbase[256];
@@ -190,13 +180,14 @@ struct LsdSmem {
 // One LSD pass over digit `slot` (skipped when that key byte is constant within every block): rank the tile's
 // suffixes by digit, publish the tile's digit counts, look back over the block's earlier tiles for the offsets
 // (bounded spin), stage the tile in shared memory in digit order and write it out in runs.
-__global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
+__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
     const Ctl *c = a.ctl;
     const u32 act = active_slots(c);
     if (!((act >> slot) & 1)) return;
-    const u32 par = __popc(act & ((1u << slot) - 1)) & 1;
+    const u32 lower = act & ((1u << slot) - 1), higher = act & ~((2u << slot) - 1);
+    const u32 par = __popc(lower) & 1;
     const u32 ntiles = c->lsd_tiles;
     const u64 epoch = (u64)((c->seq << 5) | (u32)slot) << 32;
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
@@ -210,21 +201,34 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     const bool head = tile == __ldg(&a.blk[tl.b].lt0);  // the block's first tile: its counts are the inclusive prefix
     // this pass's first position of digit tid in the block
     const u32 dbase = __ldg(a.lbase + ((u64)tl.b * NSLOT + slot) * 256 + tid);
-    const u32 *vin = a.lval[par], *khin = a.lkh[par], *klin = a.lkl[par];
+    const u32 *vin = a.lval[par], *kin = a.lkey[par];
     // rk[j]: rank in the warp's digit bucket (bits 0..15) | digit, 0x100 past the end (bits 16..24)
-    u32 v[LSD_IPT], rk[LSD_IPT], kh[LSD_IPT], kl[LSD_IPT];
+    u32 v[LSD_IPT], rk[LSD_IPT], k[LSD_IPT];
+    if (!lower) {
+        // the first pass: the tile's suffixes are still in text order, ids and keys come from the text
+        const BlockInfo bi = a.blk[tl.b];
+        const u32 id0 = bi.off + (base - bi.soff);
+        const u64 end = (u64)bi.off + bi.n;
+        const u32 g = lsd_slot_group(slot);
 #pragma unroll
-    for (int j = 0; j < LSD_IPT; j++) {
-        const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        const bool ok = x < cnt;
-        v[j] = ok ? __ldcs(vin + base + x) : 0u;
-        kh[j] = ok ? __ldcs(khin + base + x) : 0u;
-        kl[j] = ok ? __ldcs(klin + base + x) : 0u;
+        for (int j = 0; j < LSD_IPT; j++) {
+            const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
+            v[j] = id0 + x;
+            k[j] = x < cnt ? lsd_group(a.T, id0 + x, g, end) : 0u;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < LSD_IPT; j++) {
+            const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
+            const bool ok = x < cnt;
+            v[j] = ok ? __ldcs(vin + base + x) : 0u;
+            k[j] = ok ? __ldcs(kin + base + x) : 0u;
+        }
     }
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        const u32 d = (((slot & 7) < 4 ? kl[j] : kh[j]) >> (8 * (slot & 3))) & 0xFFu;
+        const u32 d = (k[j] >> (8 * (slot & 3))) & 0xFFu;  // byte 15 - slot of the prefix
         rk[j] = (x < cnt ? d : 0x100u) << 16;
     }
 #pragma unroll
@@ -259,8 +263,7 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
         if (d < 256) {
             const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFFu);
             S.val[p] = v[j];
-            S.kh[p] = kh[j];
-            S.kl[p] = kl[j];
+            S.key[p] = k[j];
             S.dg[p] = (u8)d;
         }
     }
@@ -301,14 +304,46 @@ __global__ void __launch_bounds__(TPB, 2) k_lsd_pass(FwdArgs a, int slot) {
     }
     S.gbase[tid] = dbase + excl - dstart;
     __syncthreads();
-    u32 *vout = a.lval[par ^ 1], *khout = a.lkh[par ^ 1], *klout = a.lkl[par ^ 1];
-    for (u32 i = tid; i < cnt; i += TPB) {
-        const u32 dst = S.gbase[S.dg[i]] + i;
-        if (KGB_OK(dst < base - (tile - __ldg(&a.blk[tl.b].lt0)) * LSD_TILE + __ldg(&a.blk[tl.b].n), &a.ctl->err,
-                   E_LIST)) {
-            __stcs(vout + dst, S.val[i]);
-            __stcs(khout + dst, S.kh[i]);
-            __stcs(klout + dst, S.kl[i]);
+    u32 *vout = a.lval[par ^ 1], *kout = a.lkey[par ^ 1];
+    const BlockInfo bi = a.blk[tl.b];
+    const u32 bend = bi.soff + bi.n;  // bound of the checked build's write checks
+    (void)bend;
+    // the key the next pass reads: this group's (carried), the next group's (gathered from the text) or none
+    const u32 g = lsd_slot_group(slot);
+    const int gn = higher ? (int)lsd_slot_group(__ffs(higher) - 1) : -1;
+    if (gn == (int)g) {
+        for (u32 i = tid; i < cnt; i += TPB) {
+            const u32 dst = S.gbase[S.dg[i]] + i;
+            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) {
+                __stcs(vout + dst, S.val[i]);
+                __stcs(kout + dst, S.key[i]);
+            }
+        }
+    } else if (gn >= 0) {
+        const u64 end = (u64)bi.off + bi.n;
+        constexpr int WB = 4;  // gathers in flight per thread
+        for (u32 i0 = tid; i0 < cnt; i0 += WB * TPB) {
+            u32 id[WB], kk[WB], dst[WB];
+#pragma unroll
+            for (int q = 0; q < WB; q++) {
+                const u32 i = i0 + q * TPB;
+                const bool ok = i < cnt;
+                id[q] = ok ? S.val[i] : 0u;
+                dst[q] = ok ? S.gbase[S.dg[i]] + i : 0u;
+                kk[q] = ok ? lsd_group(a.T, id[q], (u32)gn, end) : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < WB; q++) {
+                if (i0 + q * TPB < cnt && KGB_OK(dst[q] < bend, &a.ctl->err, E_LIST)) {
+                    __stcs(vout + dst[q], id[q]);
+                    __stcs(kout + dst[q], kk[q]);
+                }
+            }
+        }
+    } else {  // the last pass: the segmentation reads ids only
+        for (u32 i = tid; i < cnt; i += TPB) {
+            const u32 dst = S.gbase[S.dg[i]] + i;
+            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(vout + dst, S.val[i]);
         }
     }
 }
@@ -355,8 +390,6 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 lane = lane_id(), warp = warp_id();
     const bool w16 = a.lsd_bytes == 16;
-    const u32 fp = lsd_final_par(a.ctl);
-    const u32 *KH = a.lkh[fp], *KL = a.lkl[fp];
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
         const uint2 br = cb < v.m ? seg_chunk_blocks(a, cb, v.m) : make_uint2(0u, 0u);
@@ -368,13 +401,15 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
             const u32 b = ok ? (br.x == br.y ? br.x : blk_of_pos(a, p, br.x, br.y)) : 0u;
             const BlockInfo bi = a.blk[b];
             const u64 end = (u64)bi.off + bi.n;
-            u64 k = ok ? ((u64)KH[p] << 32) | KL[p] : 0ull;
-            // the second 8-byte word of the prefix (W = 16), from the text
-            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)v.val[p] + 8, end) : 0ull;
+            // the prefix's two 8-byte words (the second for W = 16 only), from the text
+            const u32 id = ok ? v.val[p] : 0u;
+            u64 k = ok ? lsd_key(a.T, id, end) : 0ull;
+            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)id + 8, end) : 0ull;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1), k2p = __shfl_up_sync(0xffffffffu, k2, 1);
             if (lane == 0 && ok && p > bi.soff) {  // the neighbour is in the same block
-                kp = ((u64)KH[p - 1] << 32) | KL[p - 1];
-                k2p = w16 ? lsd_key(a.T, (u64)v.val[p - 1] + 8, end) : 0ull;
+                const u32 idp = v.val[p - 1];
+                kp = lsd_key(a.T, idp, end);
+                k2p = w16 ? lsd_key(a.T, (u64)idp + 8, end) : 0ull;
             }
             const bool st = ok && (p == bi.soff || k != kp || k2 != k2p);
             const u32 sb = __ballot_sync(0xffffffffu, st);
