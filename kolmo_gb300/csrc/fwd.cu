@@ -110,6 +110,18 @@ __device__ __forceinline__ u32 rank_key(const u32 *__restrict__ isa, u32 i, u32 
 
 // The final state of a suffix: rank = suffix-array position p (block-local), L column row p + 1 = T[i - 1]
 // (the sentinel row's byte value is never read), optional suffix array, and its index in the resolved list.
+// As resolve, with the block's descriptor and the L-column byte (T[id - 1], 0 for the block's first suffix) already
+// loaded: callers load the bytes of several finished suffixes at once.
+__device__ __forceinline__ void resolve_byte(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, const BlockInfo &B,
+                                             ListView res, u32 ridx, u8 byte) {
+    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
+        return;
+    isa_nxt[id] = p;
+    a.L[(u64)B.off + b + p + 1] = byte;
+    if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
+    res.eid[ridx] = id;
+    res.ekey[ridx] = p;
+}
 __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, ListView res,
                                         u32 ridx) {
     BlockInfo B = a.blk[b];
@@ -873,6 +885,18 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         u32 gi = __shfl_sync(0xffffffffu, sbase, 0) + (excl & 0xFFFF);
         u32 r = __shfl_sync(0xffffffffu, rbase, 0) + (excl >> 16);
         const bool skip_rank = (g.bd & STABLE) && unsplit;
+        // the L-column bytes of the finished suffixes, all loads in flight before any write
+        BlockInfo bi{};
+        u8 tv[GTINY];
+        if (n1) bi = a.blk[b];
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            tv[q] = 0;
+            if (q >= len) continue;
+            const bool st = q == 0 || k[q] != k[q - 1];
+            const bool en = q + 1 == len || k[q] != k[q + 1];
+            if (st && en && v[q] != bi.off) tv[q] = __ldg(a.T + v[q] - 1);
+        }
         // a group that split is rewritten in sorted order, so that each surviving run is contiguous in its slots
         if (!unsplit && len) {
 #pragma unroll
@@ -887,7 +911,7 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
             const bool en = q + 1 == len || k[q] != k[q + 1];
             if (st) rs = q;
             if (st && en) {
-                resolve(a, isa_nxt, v[q], g.head + q, b, res, r++);
+                resolve_byte(a, isa_nxt, v[q], g.head + q, b, bi, res, r++, tv[q]);
                 continue;
             }
             const u32 head = g.head + rs;
