@@ -730,7 +730,7 @@ def main():
     ap.add_argument("--small-group", type=int, default=-1)
     ap.add_argument("--warp-path", type=int, default=-1)
     ap.add_argument("--lsd-round0", type=int, default=-1)
-    ap.add_argument("--lsd-bytes", type=int, default=-1, help="prefix bytes of the LSD round 0 (8 or 16)")
+    ap.add_argument("--lsd-bytes", type=int, default=-1, help="prefix bytes of the LSD round 0 (8, 12 or 16)")
     ap.add_argument("--profile-out", default="", help="write the per-launch profile of the profiled step here")
     ap.add_argument("--plain", action="store_true",
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")

@@ -91,7 +91,8 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
  * KGBWT_OPT_WARP_PATH (0/1, default 1): tiles whose groups are all at most 32 long go to the warp-level kernel.
  * KGBWT_OPT_LSD_ROUND0 (0/1, default 1): the first round (all suffixes by their prefix) is one LSD radix sort of the
  *   whole batch; 0: bucket passes and tile kernels over 8-byte prefixes as in the later rounds.
- * KGBWT_OPT_LSD_BYTES (8 or 16, default 16): prefix bytes that LSD round sorts (16 replaces the first rank round). */
+ * KGBWT_OPT_LSD_BYTES (8, 12 or 16, default 16): prefix bytes that LSD round sorts (16 replaces the first rank round;
+ *   the rank rounds then double from there). */
 #define KGBWT_OPT_SMALL_GROUP 1
 #define KGBWT_OPT_WARP_PATH 2
 #define KGBWT_OPT_LSD_ROUND0 3

@@ -7,7 +7,7 @@ tuning_gb300.json beside this package). Results never depend on the configuratio
 Tuned per bucket: CTAs per SM of the block tile kernel (tile_ctas) and of the bucket passes (msd_ctas), the
 counting-sort threshold of the tile kernel (small_group), the warp-level tile path (warp_path), the round-0 path
 (lsd_round0: one LSD radix sort of all suffixes, or bucket passes + tiles) and the prefix it sorts (lsd_bytes: 16,
-which spares the first rank round, or 8). The tile capacity changes the workspace layout and is left at its default.
+which spares the first rank round, 12 or 8). The tile capacity changes the workspace layout and is left at its default.
 """
 from __future__ import annotations
 
@@ -37,7 +37,7 @@ BUCKETS = [
 
 CANDIDATES = {
     "lsd_round0": (1, 0),
-    "lsd_bytes": (16, 8),
+    "lsd_bytes": (16, 12, 8),
     "msd_ctas": (8, 4),
     "tile_ctas": (2, 1),
     "small_group": (64, 0),

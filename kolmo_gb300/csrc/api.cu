@@ -302,7 +302,7 @@ static int parse_tuning(const char *text, std::vector<TuneBucket> &out) {
             else if (key == "small_group") { if (v < 0 || v > 1024) return -1; b.c.small_group = (int)v; }
             else if (key == "warp_path") { if (v != 0 && v != 1) return -1; b.c.warp_path = (int)v; }
             else if (key == "lsd_round0") { if (v != 0 && v != 1) return -1; b.c.lsd_round0 = (int)v; }
-            else if (key == "lsd_bytes") { if (v != 8 && v != 16) return -1; b.c.lsd_bytes = (int)v; }
+            else if (key == "lsd_bytes") { if (v != 8 && v != 12 && v != 16) return -1; b.c.lsd_bytes = (int)v; }
         }
         if (!have_max) return -1;
         out.push_back(b);
@@ -448,7 +448,7 @@ int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
             e->fwd.cfg_explicit |= CFG_LSD_ROUND0;
             return 0;
         case KGBWT_OPT_LSD_BYTES:
-            if (value != 8 && value != 16) return -1;
+            if (value != 8 && value != 12 && value != 16) return -1;
             e->fwd.ucfg.lsd_bytes = value;
             e->fwd.cfg_explicit |= CFG_LSD_BYTES;
             return 0;

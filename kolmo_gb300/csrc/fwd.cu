@@ -62,7 +62,7 @@ struct FwdArgs {
     u32 B;
     u32 smax;
     u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
-    u32 lsd_bytes;    // prefix bytes of the LSD round 0 (8 or 16)
+    u32 lsd_bytes;    // prefix bytes of the LSD round 0 (8, 12 or 16)
     u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort

@@ -70,7 +70,7 @@ struct FwdConfig {
     int small_group = 64; // tiles whose groups are all at most this long skip the radix passes (counting sort)
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
     int lsd_round0 = 1;   // round 0 as one LSD radix sort of all suffixes; 0: bucket passes + tiles over 8-byte prefixes
-    int lsd_bytes = 16;   // prefix bytes the LSD round 0 sorts (8 or 16)
+    int lsd_bytes = 16;   // prefix bytes the LSD round 0 sorts (8, 12 or 16)
 };
 // Fields of FwdConfig a caller set explicitly (they override the tuning table).
 enum : u32 {

@@ -1,5 +1,5 @@
 // Round 0 of the forward sort as one LSD radix sort: the suffixes of each block of the batch are sorted by their
-// zero-padded W-byte prefix, W = 16 (or 8), with one pass per varying key byte (single-pass scatter with decoupled
+// zero-padded W-byte prefix, W = 16 (or 12 or 8), with one pass per varying key byte (single-pass scatter with decoupled
 // look-back), then a segmentation turns the sorted order into ranks, finished suffixes and the rank rounds' groups
 // (tiny, medium, small and large lists). The sort tiles never straddle two blocks: every block's suffixes keep their
 // own range of the dense order (the block's soff onward), a pass takes each tile's digit bases from its own block's
@@ -125,12 +125,12 @@ __global__ void __launch_bounds__(TPB) k_lsd_key0(FwdArgs a) {
 // Suffix i of a block of n bytes has key byte d = T[i + d] when i + d < n, else 0, so the counts of key byte d are
 // the block's byte counts minus those of its first min(d, n) bytes, plus min(d, n) zeros; their exclusive scan plus
 // the block's soff gives the pass's first position of every digit (lbase row (block, slot), slot = 15 - d). A slot
-// runs when its key byte takes two or more values within some block (slots 8..15 only for W = 8).
+// runs when its key byte takes two or more values within some block (slots 16 - W..15 only).
 __global__ void __launch_bounds__(TPB) k_lsd_hist0(FwdArgs a) {
     __shared__ u32 wm[8];
     __shared__ u32 ws[TPB / 32 + 1];
     const u32 x = threadIdx.x;
-    const int first = a.lsd_bytes == 16 ? 0 : 8;
+    const int first = 16 - (int)a.lsd_bytes;
     for (u32 b = blockIdx.x; b < a.B; b += gridDim.x) {
         const BlockInfo bi = a.blk[b];
         const u32 h = a.lhist[(u64)b * 256 + x];
@@ -389,7 +389,9 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     const SegBufs v = seg_bufs(a);
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 lane = lane_id(), warp = warp_id();
-    const bool w16 = a.lsd_bytes == 16;
+    // the prefix's second 8-byte word: its first W - 8 bytes (none for W = 8)
+    const u64 m2 = a.lsd_bytes >= 16 ? ~0ull : a.lsd_bytes == 12 ? 0xFFFFFFFF00000000ull : 0ull;
+    const bool w16 = m2 != 0;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
         const uint2 br = cb < v.m ? seg_chunk_blocks(a, cb, v.m) : make_uint2(0u, 0u);
@@ -401,15 +403,15 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
             const u32 b = ok ? (br.x == br.y ? br.x : blk_of_pos(a, p, br.x, br.y)) : 0u;
             const BlockInfo bi = a.blk[b];
             const u64 end = (u64)bi.off + bi.n;
-            // the prefix's two 8-byte words (the second for W = 16 only), from the text
+            // the prefix's two 8-byte words (the second cut to its first W - 8 bytes), from the text
             const u32 id = ok ? v.val[p] : 0u;
             u64 k = ok ? lsd_key(a.T, id, end) : 0ull;
-            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)id + 8, end) : 0ull;
+            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)id + 8, end) & m2 : 0ull;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1), k2p = __shfl_up_sync(0xffffffffu, k2, 1);
             if (lane == 0 && ok && p > bi.soff) {  // the neighbour is in the same block
                 const u32 idp = v.val[p - 1];
                 kp = lsd_key(a.T, idp, end);
-                k2p = w16 ? lsd_key(a.T, (u64)idp + 8, end) : 0ull;
+                k2p = w16 ? lsd_key(a.T, (u64)idp + 8, end) & m2 : 0ull;
             }
             const bool st = ok && (p == bi.soff || k != kp || k2 != k2p);
             const u32 sb = __ballot_sync(0xffffffffu, st);

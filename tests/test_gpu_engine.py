@@ -87,9 +87,9 @@ def test_engine_configs_give_identical_results():
         assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
 
 
-@pytest.mark.parametrize("lsd_round0,lsd_bytes", [(0, 16), (1, 8), (1, 16)])
+@pytest.mark.parametrize("lsd_round0,lsd_bytes", [(0, 16), (1, 8), (1, 12), (1, 16)])
 def test_round0_paths_on_mixed_batch(lsd_round0, lsd_bytes):
-    """Round 0 as one LSD radix sort of the batch (over 8- or 16-byte prefixes, sort tiles aligned to the blocks), or
+    """Round 0 as one LSD radix sort of the batch (over 8-, 12- or 16-byte prefixes, sort tiles aligned to the blocks), or
     as bucket passes + tiles: each must give the oracle's L column and sampled indexes, on a batch that mixes two-byte
     blocks (the engine's minimum), blocks shorter than the prefix, runs longer than a tile (large groups spanning
     segmentation tiles) and ordinary text."""
