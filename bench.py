@@ -195,14 +195,14 @@ TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 21.6}
 def algorithmic_bytes(rec: dict) -> float:
     """Algorithmic bytes of one launch (the per-unit figures of the doubling model): a rank round costs 48 B per
     active suffix (read its id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id),
-    a round-0 radix pass 24 B per suffix (read and write its 12 B item: id and one 8-byte key word), the inverse 10 B
+    a round-0 radix pass 16 B per suffix (read and write its 8 B item: id and one 4-byte key group), the inverse 10 B
     per byte over its passes (psi build: read L, write psi; walk: read psi, write text)."""
     k, e = rec["kernel"], rec["elems"]
     if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed", "group_thread",
              "group_warp"):
         return 48.0 * e
     if k == "lsd_pass":
-        return 24.0 * e  # every pass reads and writes each suffix's 12 B item
+        return 16.0 * e  # every pass reads and writes each suffix's 8 B item
     if k in ("tile_sort_prefix", "tile_sort_prefix_keyed", "tile_warp_prefix", "tile_warp_prefix_keyed"):
         return 33.0 * e
     if k == "inv_walk":
@@ -356,7 +356,7 @@ def run_ours(args, world, rank, local):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "launches_per_step": dd["launches"], "share": round(dd["ms"] / tot_ms, 4),
-                     "bytes_model": "rank round 48 B per active suffix, round-0 radix pass 24 B per suffix (per "
+                     "bytes_model": "rank round 48 B per active suffix, round-0 radix pass 16 B per suffix (per "
                                     "launch: elements of the launch's work list)"},
         "kernel_shares": {k: round(v["ms"] / tot_ms, 4) for k, v in sorted(by_kernel.items(), key=lambda x: -x[1]["ms"])},
         "rounds": round_table,

@@ -32,7 +32,7 @@ BUCKETS = [
     ("prose 4 MiB", [("prose", 4 * MIB)]),
     ("prose 16 MiB", [("prose", 16 * MIB)]),
     ("prose 64 MiB", [("prose", 64 * MIB)]),
-    ("16 mixed blocks of 16 MiB", [(k % 3, 16 * MIB) for k in range(16)]),
+    ("96 mixed blocks, log-uniform 16 KiB-16 MiB", "mixed96"),
 ]
 
 CANDIDATES = {
@@ -46,6 +46,8 @@ CANDIDATES = {
 
 
 def _batch(spec, seed):
+    if spec == "mixed96":  # the mixed batch's shape (sources and size law) on another seed
+        return [t for _, t in W.mixed_batch(96, seed=seed)]
     texts = []
     for k, (src, n) in enumerate(spec):
         texts.append(W.zipf_prose(n, seed + k) if src == "prose" else W.source_block(src, n, seed + k))
