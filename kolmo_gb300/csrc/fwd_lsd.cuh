@@ -170,7 +170,6 @@ __global__ void __launch_bounds__(TPB) k_lsd_ident(FwdArgs a) {
 struct LsdSmem {
     u32 val[LSD_TILE];
     u32 key[LSD_TILE];
-    u8 dg[LSD_TILE];
     u16 wcnt[TPB / 32][256];
     u32 gbase[256];
     u32 ws[TPB / 32 + 1];
@@ -202,8 +201,10 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     // this pass's first position of digit tid in the block
     const u32 dbase = __ldg(a.lbase + ((u64)tl.b * NSLOT + slot) * 256 + tid);
     const u32 *vin = a.lval[par], *kin = a.lkey[par];
-    // rk[j]: rank in the warp's digit bucket (bits 0..15) | digit, 0x100 past the end (bits 16..24)
-    u32 v[LSD_IPT], rk[LSD_IPT], k[LSD_IPT];
+    // rr: each item's rank in its warp's digit bucket (< 512), two 16-bit ranks per register; the digit itself is
+    // recomputed from the key where it is needed
+    u32 v[LSD_IPT], rr[LSD_IPT / 2], k[LSD_IPT];
+    const u32 dsh = 8 * (slot & 3);  // byte 15 - slot of the prefix within the key group
     if (!lower) {
         // the first pass: the tile's suffixes are still in text order, ids and keys come from the text
         const BlockInfo bi = a.blk[tl.b];
@@ -228,15 +229,11 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        const u32 d = (k[j] >> (8 * (slot & 3))) & 0xFFu;  // byte 15 - slot of the prefix
-        rk[j] = (x < cnt ? d : 0x100u) << 16;
-    }
-#pragma unroll
-    for (int j = 0; j < LSD_IPT; j++) {
-        const u32 d = rk[j] >> 16;
+        const u32 d = x < cnt ? (k[j] >> dsh) & 0xFFu : 0x100u;  // 0x100: past the tile's end
         const u32 peers = __match_any_sync(0xffffffffu, d);
         const u32 before = d < 256 ? S.wcnt[warp][d] : 0u;
-        rk[j] |= before + __popc(peers & lanemask_lt());
+        const u32 r = before + __popc(peers & lanemask_lt());
+        if (j & 1) rr[j >> 1] |= r << 16; else rr[j >> 1] = r;
         __syncwarp();
         if (d < 256 && (__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
         __syncwarp();
@@ -259,12 +256,12 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     // stage in digit order (tile-local offsets only: the items leave registers before the look-back)
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
-        const u32 d = rk[j] >> 16;
-        if (d < 256) {
-            const u32 p = S.wcnt[warp][d] + (rk[j] & 0xFFFFu);
+        const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
+        if (x < cnt) {
+            const u32 d = (k[j] >> dsh) & 0xFFu;
+            const u32 p = S.wcnt[warp][d] + ((rr[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
             S.val[p] = v[j];
             S.key[p] = k[j];
-            S.dg[p] = (u8)d;
         }
     }
     u32 excl = 0;
@@ -313,7 +310,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     const int gn = higher ? (int)lsd_slot_group(__ffs(higher) - 1) : -1;
     if (gn == (int)g) {
         for (u32 i = tid; i < cnt; i += TPB) {
-            const u32 dst = S.gbase[S.dg[i]] + i;
+            const u32 dst = S.gbase[(S.key[i] >> dsh) & 0xFFu] + i;
             if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) {
                 __stcs(vout + dst, S.val[i]);
                 __stcs(kout + dst, S.key[i]);
@@ -329,7 +326,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
                 const u32 i = i0 + q * TPB;
                 const bool ok = i < cnt;
                 id[q] = ok ? S.val[i] : 0u;
-                dst[q] = ok ? S.gbase[S.dg[i]] + i : 0u;
+                dst[q] = ok ? S.gbase[(S.key[i] >> dsh) & 0xFFu] + i : 0u;
                 kk[q] = ok ? lsd_group(a.T, id[q], (u32)gn, end) : 0u;
             }
 #pragma unroll
@@ -342,7 +339,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         }
     } else {  // the last pass: the segmentation reads ids only
         for (u32 i = tid; i < cnt; i += TPB) {
-            const u32 dst = S.gbase[S.dg[i]] + i;
+            const u32 dst = S.gbase[(S.key[i] >> dsh) & 0xFFu] + i;
             if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(vout + dst, S.val[i]);
         }
     }
