@@ -188,8 +188,9 @@ def prose_block(rank: int, mib: int = 64):
 
 # DRAM bytes per unit (suffix) measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 16 MiB prose
 # case: profiles/traffic_group_thread_lsd_pass_prose16.md (tiny groups) and profiles/lsd_pass_prose16.md (the
-# keyed round-0 pass). The 64 MiB launch's traffic is scaled by the suffixes it processes.
-TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 21.6}
+# round-0 radix pass, averaged over a 16-pass step). The 64 MiB launch's traffic is scaled by the suffixes it
+# processes.
+TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 13.9}
 
 
 def algorithmic_bytes(rec: dict) -> float:
