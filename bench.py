@@ -376,12 +376,30 @@ def run_ours(args, world, rank, local):
     return out
 
 
+SLICE_BYTES, SLICE_COUNT = 512 << 10, 128
+
+
+def batch_blocks(workload: str):
+    """The blocks of a batch workload and its description: the mixed batch (256 blocks of 16 KiB-16 MiB,
+    log-uniform; order-2 Markov, ACGT with 0.1% N, templated log lines), or the -9 slice trials (128 consecutive
+    512 KiB slices of the 64 MiB prose block, each sorted on its own, as the level-9 planner sorts trial slices of a
+    file: src/core/blocks.c:399-517)."""
+    from kolmo_gb300 import workloads as W
+
+    if workload == "slices":
+        T = W.prose_64mib()
+        texts = [T[i * SLICE_BYTES:(i + 1) * SLICE_BYTES] for i in range(SLICE_COUNT)]
+        return texts, (f"slices{SLICE_COUNT}: {SLICE_COUNT} consecutive {SLICE_BYTES >> 10} KiB slices of the 64 MiB "
+                       "prose block (the -9 slice trials), forward + inverse BWT, one graph launch per direction")
+    return [t for _, t in W.mixed_batch()], ("batch256: 256 blocks, log-uniform 16 KiB-16 MiB (order-2 Markov, "
+                                             "ACGT, log lines), forward + inverse BWT, one graph launch per direction")
+
+
 def run_batch(args, world, rank, local):
-    """The mixed batch (256 blocks of 16 KiB-16 MiB, log-uniform; order-2 Markov, ACGT with 0.1% N, templated log
-    lines): one step = forward + inverse of every block. Timed three ways: the batched graph path (one engine call
-    per direction for the whole batch, device-resident buffers), the plain per-block path (one call per block,
-    host-driven rounds), and e2e through the batch C ABI (kgbwt_fwd_batch / kgbwt_inv_batch, host buffers). Each
-    rank takes a longest-first share of the blocks (weak scaling by blocks, no collective)."""
+    """A batch workload (batch_blocks): one step = forward + inverse of every block. Timed three ways: the batched
+    graph path (one engine call per direction for the whole batch, device-resident buffers), the plain per-block path
+    (one call per block, host-driven rounds), and e2e through the batch C ABI (kgbwt_fwd_batch / kgbwt_inv_batch,
+    host buffers). Each rank takes a longest-first share of the blocks (weak scaling by blocks, no collective)."""
     import torch
 
     from kolmo_gb300 import codec, native
@@ -390,9 +408,9 @@ def run_batch(args, world, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    allb = W.mixed_batch()
-    mine = shard([int(t.size) for _, t in allb], rank, world)
-    texts = [allb[i][1] for i in mine]
+    allb, wname = batch_blocks(args.workload)
+    mine = shard([int(t.size) for t in allb], rank, world)
+    texts = [np.ascontiguousarray(allb[i]) for i in mine]
     offs, o = [], 0
     for t in texts:
         offs.append(o)
@@ -509,8 +527,7 @@ def run_batch(args, world, rank, local):
         "metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tb / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "batch256: 256 blocks, log-uniform 16 KiB-16 MiB (order-2 Markov, ACGT, log lines), "
-                               "forward + inverse BWT, one graph launch per direction",
+        "config": {"workload": wname,
                    "blocks": len(texts), "bytes": total, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"blocks sharded longest-first over {world} rank(s)"},
         "plain_per_block_MiB_per_s": round(plain_v, 2),
@@ -720,7 +737,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch", "serve"])
+    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch", "slices", "serve"])
     ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests per second)")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
     ap.add_argument("--slots", type=int, default=3, help="serve: server workers")
@@ -747,7 +764,7 @@ def main():
     import torch
 
     dist_init(world, "nccl" if torch.cuda.is_available() else "gloo")
-    if args.workload == "batch":
+    if args.workload in ("batch", "slices"):
         out = run_batch(args, world, rank, local)
     elif args.workload == "serve":
         out = run_serve(args, world, rank, local)
