@@ -1474,14 +1474,28 @@ __global__ void __launch_bounds__(TPB) k_msd_scatter(FwdArgs a) {
     }
 }
 
-// The suffixes resolved in the previous round: copy their final rank into this round's write buffer.
+// The suffixes resolved in the previous round: copy their final rank into this round's write buffer (one by one from
+// the resolved list, or, when they are many, by copying the whole current buffer).
 __global__ void __launch_bounds__(TPB) k_fixup(FwdArgs a) {
     const Ctl *ctl = a.ctl;
     const u32 rpar = ctl->rpar;
     const ListView r = a.lists[L_R0 + (rpar ^ 1)];
     const u32 n = min((u32)ctl->cnt[L_R0 + (rpar ^ 1)], (u32)a.cap_n);
     u32 *nxt = a.isa[rpar ^ 1];
-    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) nxt[r.eid[i]] = r.ekey[i];
+    const u32 idn = min(ctl->idn, (u32)a.cap_n);
+    const u32 stride = gridDim.x * TPB;
+    if ((u64)n * 16 > idn) {
+        // many suffixes finished last round: copy the whole current rank buffer instead of scattering them (every
+        // suffix's current rank, which this round's kernels then overwrite for the active ones); a streaming copy
+        // costs far less than millions of random 4-byte writes
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.isa[rpar]);
+        uint4 *dst = reinterpret_cast<uint4 *>(nxt);
+        const u32 n4 = idn / 4;
+        for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n4; i += stride) __stcs(dst + i, __ldcs(src + i));
+        for (u32 i = n4 * 4 + blockIdx.x * TPB + threadIdx.x; i < idn; i += stride) nxt[i] = a.isa[rpar][i];
+        return;
+    }
+    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += stride) nxt[r.eid[i]] = r.ekey[i];
 }
 
 // ------------------------------------------------------------------------------------------------ control
@@ -1820,6 +1834,7 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     c.seq = ++call_seq;
     c.h0 = lsd_enabled() ? (u32)cfg.lsd_bytes : 8u;
     c.lsd_tiles = lt_b;
+    for (u32 b = 0; b < B; b++) c.idn = std::max(c.idn, h_off[b] + h_n[b]);
     KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
     const size_t ntm = cap_tms;
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemsetAsync(lists[l].tbig, 0xFF, ntm * 4, s));

@@ -61,6 +61,7 @@ struct Ctl {
     u32 m;              // suffixes sorted
     u32 seq;            // call sequence number (tags the look-back words of the radix passes)
     u32 p_alloc;        // slots taken so far in the tiny-group id array (shared by both parities, never reused)
+    u32 idn;            // suffix ids of the batch lie in [0, idn) (the rank buffers' used extent)
 };
 
 struct FwdConfig {
