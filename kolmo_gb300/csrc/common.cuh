@@ -121,7 +121,7 @@ enum KernelId : int {
     K_INIT, K_FIXUP, K_KEYGEN, K_MSD_HIST, K_MSD_SCAN, K_MSD_SCATTER, K_TILE_PREFIX, K_TILE_PREFIX_KEYED,
     K_TILE_RANK, K_TILE_RANK_KEYED, K_CTL, K_SAMPLES,
     K_WARP_PREFIX, K_WARP_PREFIX_KEYED, K_WARP_RANK, K_WARP_RANK_KEYED,
-    K_LSD_BEGIN, K_LSD_KEY0, K_LSD_HIST, K_LSD_PASS, K_SEG_COUNT, K_SEG_SCAN, K_SEG_EMIT1, K_SEG_EMIT2, K_GROUP, K_GROUP_WARP, K_MKEYS, K_LSD_IDENT,
+    K_LSD_BEGIN, K_LSD_KEY0, K_LSD_HIST, K_LSD_PASS, K_SEG_COUNT, K_SEG_SCAN, K_SEG_EMIT1, K_SEG_EMIT2, K_GROUP, K_GROUP_WARP, K_MKEYS, K_LSD_IDENT, K_SEG_RANK,
     K_INV_TILEHIST, K_INV_COLSCAN, K_INV_SCATTER, K_INV_WALK, K_INV_RANKINIT, K_INV_JUMP, K_INV_EMIT, K_NKERNELS
 };
 const char *kernel_name(int k);

@@ -63,6 +63,8 @@ struct FwdArgs {
     u32 smax;
     u32 small_group;  // tiles whose groups are all at most this long are sorted by counting, not radix passes
     u32 lsd_bytes;    // prefix bytes of the LSD round 0 (8, 12 or 16)
+    u32 idn;          // suffix ids of the batch lie in [0, idn)
+    u32 rank_passes;  // round 0's ranks: passes of k_seg_rank over id ranges, or 0: written by the emit kernels
     u32 warp_path;    // 1: tiles without a group longer than WARP_GROUP belong to the warp-level kernel
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
@@ -118,6 +120,16 @@ __device__ __forceinline__ void resolve_byte(const FwdArgs &a, u32 *isa_nxt, u32
         return;
     isa_nxt[id] = p;
     a.L[(u64)B.off + b + p + 1] = byte;
+    if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
+    res.eid[ridx] = id;
+    res.ekey[ridx] = p;
+}
+// As resolve, without the rank write (round 0 writes every suffix's rank in a separate pass).
+__device__ __forceinline__ void resolve_norank(const FwdArgs &a, u32 id, u32 p, u32 b, ListView res, u32 ridx) {
+    BlockInfo B = a.blk[b];
+    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
+        return;
+    a.L[(u64)B.off + b + p + 1] = id == B.off ? 0 : __ldg(a.T + id - 1);
     if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
     res.eid[ridx] = id;
     res.ekey[ridx] = p;
@@ -1725,6 +1737,13 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.lsd_bytes = (u32)cfg.lsd_bytes;
+    a.idn = (u32)N;
+    {
+        // the emit kernels' rank writes stay within one block's ids at a time (the sorted order is block-major), so
+        // they only miss L2 when a block is larger than a pass's span
+        const u64 p = (N + RANK_SPAN - 1) / RANK_SPAN;
+        a.rank_passes = maxn > RANK_SPAN && p <= RANK_PASSES_MAX ? (u32)p : 0u;
+    }
     a.warp_path = (u32)cfg.warp_path;
     a.cap_n = Ncap; a.cap_segs = cap_segs; a.cap_segk = cap_segk; a.cap_segl = cap_segl; a.cap_segt = cap_segt;
     a.cap_segm = cap_segm;
@@ -1834,7 +1853,7 @@ int FwdEngine::setup_round0(cudaStream_t s) {
     c.seq = ++call_seq;
     c.h0 = lsd_enabled() ? (u32)cfg.lsd_bytes : 8u;
     c.lsd_tiles = lt_b;
-    for (u32 b = 0; b < B; b++) c.idn = std::max(c.idn, h_off[b] + h_n[b]);
+    c.idn = (u32)N;  // N is the batch's extent: max over blocks of off + n
     KGB_CHECK(cudaMemcpyAsync(d_blk, bi.data(), B * sizeof(BlockInfo), cudaMemcpyHostToDevice, s));
     const size_t ntm = cap_tms;
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemsetAsync(lists[l].tbig, 0xFF, ntm * 4, s));
@@ -2039,7 +2058,12 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
     L.tag(K_SEG_EMIT1, m_tag);
     if ((e = L.go(k_seg_emit1, L.grid_msd, TPB, 0, a))) return e;
     L.tag(K_SEG_EMIT2, m_tag);
-    return L.go(k_seg_emit2, L.grid_msd, TPB, 0, a);
+    if ((e = L.go(k_seg_emit2, L.grid_msd, TPB, 0, a))) return e;
+    for (u64 lo = 0; a.rank_passes && lo < a.idn; lo += RANK_SPAN) {
+        L.tag(K_SEG_RANK, m_tag);
+        if ((e = L.go(k_seg_rank, L.grid_msd, TPB, 0, a, (u32)lo, (u32)std::min<u64>(lo + RANK_SPAN, a.idn)))) return e;
+    }
+    return cudaSuccess;
 }
 
 static u32 host_active_slots(const Ctl &c) { return c.lsd_act; }

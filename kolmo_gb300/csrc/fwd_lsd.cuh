@@ -512,7 +512,8 @@ __device__ __forceinline__ u64 block_excl_sum64(u64 v, u64 *ws, u64 *total) {
     return before + inc - v;
 }
 
-// Emit, part 1 (group ends): groups of one resolve; every other group takes its slots in the next tiny-group list
+// Emit, part 1 (group ends): groups of one resolve (rank unless k_seg_rank writes the ranks, L column, resolved
+// list); every other group takes its slots in the next tiny-group list
 // (<= GTINY), medium-group list (<= GMED), small-group list (<= SMAX) or large-group list, writes its descriptor (and
 // tile-map entries), and records its slot base and index at its first position for part 2. Slots are allocated once
 // per tile (a count pass, a block scan, one atomic per list).
@@ -526,7 +527,6 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
     const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
     const ListView res = a.lists[L_R0 + rpar];
-    u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 TS = a.smax;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -598,7 +598,8 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
                 const u32 b = bv[q];
                 const u32 head = gf - a.blk[b].soff;
                 if (len == 1) {
-                    resolve(a, isa_nxt, idv[q], head, b, res, r1++);
+                    if (!a.rank_passes && idv[q] < a.cap_n) a.isa[rpar ^ 1][idv[q]] = head;
+                    resolve_norank(a, idv[q], head, b, res, r1++);
                     continue;
                 }
                 Seg g;
@@ -644,8 +645,9 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     }
 }
 
-// Emit, part 2 (every suffix of a group of two or more): its rank (the group's first position), its slot in its
-// group's list, and for large groups the bucket-pass tile map (the suffix at a multiple of TSM names its group).
+// Emit, part 2 (every suffix of a group of two or more): its rank (the group's first position) unless k_seg_rank
+// writes the ranks, its slot in its group's list, and for large groups the bucket-pass tile map (the suffix at a
+// multiple of TSM names its group).
 __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
     __shared__ u32 wl[TPB / 32];
     Ctl *c = a.ctl;
@@ -653,7 +655,6 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
     const u32 rpar = c->rpar;
     const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
     const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
-    u32 *isa_nxt = a.isa[rpar ^ 1];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     constexpr int QB = 8;  // positions per phase: group starts first, then every load, then every store
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -668,12 +669,11 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
                 pv[q] = p; gfv[q] = gf;
                 if (ok && !(st && en)) live |= 1u << q;  // groups of one were resolved by part 1
             }
-            u32 idv[QB], giv[QB], gbv[QB], bv[QB];
+            u32 idv[QB], giv[QB], gbv[QB];
 #pragma unroll
             for (int q = 0; q < QB; q++) {
                 if (!((live >> q) & 1)) continue;
                 idv[q] = __ldg(v.val + pv[q]);
-                bv[q] = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, pv[q], ch.blo, ch.bhi);
                 giv[q] = __ldg(v.gidx + gfv[q]);
                 gbv[q] = __ldg(v.gbase + gfv[q]);
             }
@@ -681,10 +681,12 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
             for (int q = 0; q < QB; q++) {
                 if (!((live >> q) & 1)) continue;
                 const u32 id = idv[q], gi = giv[q], p = pv[q], gf = gfv[q];
-                const u32 head = gf - a.blk[bv[q]].soff;
                 const u32 slot = gbv[q] + (p - gf);
                 KGB_GUARD(id < a.cap_n && slot < a.cap_n, &c->err, E_LIST) {
-                    isa_nxt[id] = head;
+                    if (!a.rank_passes) {
+                        const u32 b = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, p, ch.blo, ch.bhi);
+                        a.isa[rpar ^ 1][id] = gf - a.blk[b].soff;
+                    }
                     if (gi & GRP_LARGE) {
                         ll.eid[slot] = id;
                         if (slot % TSM == 0) {
@@ -699,6 +701,39 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
                     }
                 }
             }
+        }
+        __syncthreads();
+    }
+}
+
+// Ranks after round 0 (every suffix: its group's first position in its block), for the suffixes whose id lies in
+// [lo, hi). The host runs one pass per id range of RANK_SPAN ids, so that the rank writes of a pass (a scatter over
+// 4 * RANK_SPAN bytes) stay in L2 and reach DRAM as whole sectors, instead of one read-modify-write per suffix;
+// every pass streams the sorted ids and the group-start bits again.
+constexpr u32 RANK_SPAN = 16u << 20;
+// More passes than this cost more streaming than the random writes they replace (about 4 ps per suffix and pass
+// against about 29 ps per random rank write, measured on a 64 MiB block): the emit kernels write the ranks instead,
+// as they do when no block exceeds RANK_SPAN suffixes (their writes then stay within one block's ids at a time).
+constexpr u32 RANK_PASSES_MAX = 4;
+__global__ void __launch_bounds__(TPB) k_seg_rank(FwdArgs a, u32 lo, u32 hi) {
+    __shared__ u32 wl[TPB / 32];
+    Ctl *c = a.ctl;
+    const SegBufs v = seg_bufs(a);
+    u32 *isa_nxt = a.isa[c->rpar ^ 1];
+    const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
+    const u32 span = hi - lo;
+    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SegChunk ch = seg_chunk(a, v, t, wl);
+        u32 carry = ch.carry0;
+#pragma unroll 4
+        for (int j = 0; j < SEG_IPT; j++) {
+            u32 p, gf; bool ok, st, en;
+            seg_step(v, ch, j, carry, p, ok, st, en, gf);
+            if (!ok) continue;
+            const u32 id = __ldcs(v.val + p);
+            if (id - lo >= span) continue;
+            const u32 b = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, p, ch.blo, ch.bhi);
+            KGB_GUARD(id < a.cap_n, &c->err, E_RANK) isa_nxt[id] = gf - a.blk[b].soff;
         }
         __syncthreads();
     }

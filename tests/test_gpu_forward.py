@@ -158,3 +158,21 @@ def test_full_size_degenerate_blocks():
         if kind in ("periodic-1", "fibonacci"):
             orc, oback = O.unbwt_aux(U, r, I)
             assert orc == 0 and np.array_equal(oback, T), kind
+
+
+@pytest.mark.parametrize("mib", [24, 64])
+def test_blocks_with_ranked_passes(mib):
+    """Blocks of more than 16 M suffixes in a batch of at most 64 M write round 0's ranks in passes over id ranges
+    (24 MiB: two passes, the last one partial; 64 MiB: four): the GPU inverse restores the text, and for 24 MiB the
+    oracle's inverse decodes the GPU's BWT and sampled indexes as well (the BWT is a bijection, so this pins the
+    forward's output)."""
+    n = mib << 20
+    T = W.zipf_prose(n, 600 + mib)
+    r = 1 << codec18_rlog(n)
+    rc, U, I = codec.bwt_aux(T, r)
+    assert rc == 0, native.last_error()
+    rc, back = codec.unbwt_aux(U, r, I)
+    assert rc == 0 and np.array_equal(back, T)
+    if mib == 24:
+        orc, oback = O.unbwt_aux(U, r, I)
+        assert orc == 0 and np.array_equal(oback, T)
