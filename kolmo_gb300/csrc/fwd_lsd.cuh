@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
     const u32 lane = lane_id(), warp = warp_id();
     // the prefix's second 8-byte word: its first W - 8 bytes (none for W = 8)
     const u64 m2 = a.lsd_bytes >= 16 ? ~0ull : a.lsd_bytes == 12 ? 0xFFFFFFFF00000000ull : 0ull;
-    const bool w16 = m2 != 0;
+    const bool two = m2 != 0;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const u32 cb = t * SEG_TILE + warp * 32 * SEG_IPT;
         const uint2 br = cb < v.m ? seg_chunk_blocks(a, cb, v.m) : make_uint2(0u, 0u);
@@ -403,12 +403,12 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
             // the prefix's two 8-byte words (the second cut to its first W - 8 bytes), from the text
             const u32 id = ok ? v.val[p] : 0u;
             u64 k = ok ? lsd_key(a.T, id, end) : 0ull;
-            u64 k2 = ok && w16 ? lsd_key(a.T, (u64)id + 8, end) & m2 : 0ull;
+            u64 k2 = ok && two ? lsd_key(a.T, (u64)id + 8, end) & m2 : 0ull;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1), k2p = __shfl_up_sync(0xffffffffu, k2, 1);
             if (lane == 0 && ok && p > bi.soff) {  // the neighbour is in the same block
                 const u32 idp = v.val[p - 1];
                 kp = lsd_key(a.T, idp, end);
-                k2p = w16 ? lsd_key(a.T, (u64)idp + 8, end) & m2 : 0ull;
+                k2p = two ? lsd_key(a.T, (u64)idp + 8, end) & m2 : 0ull;
             }
             const bool st = ok && (p == bi.soff || k != kp || k2 != k2p);
             const u32 sb = __ballot_sync(0xffffffffu, st);

@@ -37,11 +37,22 @@ def test_bucket_lookup(tmp_path, restore_table):
 
 def test_malformed_tables_are_refused(tmp_path, restore_table):
     for bad in ('{"no": []}', '{"buckets": [{"tile_ctas": 2}]}', '{"buckets": [{"max_bytes": 10, "msd_ctas": 99}]}',
-                '{"buckets": [{"max_bytes": 10, "warp_path": 2}]}', 'not json'):
+                '{"buckets": [{"max_bytes": 10, "warp_path": 2}]}', '{"buckets": [{"max_bytes": 10, "lsd_bytes": 10}]}',
+                'not json'):
         p = tmp_path / "bad.json"
         p.write_text(bad)
         assert codec.tuning_load(p) == -1
     assert codec.tuning_load(tmp_path / "missing.json") == -1
+
+
+def test_prefix_widths(tmp_path, restore_table):
+    """Round 0 sorts 8-, 12- or 16-byte prefixes; a bucket without the field keeps the default (16)."""
+    t = {"buckets": [{"max_bytes": 1 << 20, "lsd_bytes": 12}, {"max_bytes": 1 << 22, "lsd_bytes": 8},
+                     {"max_bytes": 1 << 30}]}
+    p = tmp_path / "w.json"
+    p.write_text(json.dumps(t))
+    assert codec.tuning_load(p) == 3
+    assert [codec.tuning_lookup(n)[1]["lsd_bytes"] for n in (1000, 2 << 20, 8 << 20)] == [12, 8, 16]
 
 
 def test_no_table_gives_defaults(restore_table):
