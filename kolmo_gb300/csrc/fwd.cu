@@ -124,15 +124,14 @@ __device__ __forceinline__ void resolve_byte(const FwdArgs &a, u32 *isa_nxt, u32
     res.eid[ridx] = id;
     res.ekey[ridx] = p;
 }
-// As resolve, without the rank write (round 0 writes every suffix's rank in a separate pass).
-__device__ __forceinline__ void resolve_norank(const FwdArgs &a, u32 id, u32 p, u32 b, ListView res, u32 ridx) {
+// As resolve, for round 0: no resolved-list entry (round 1's fixup copies the whole rank buffer) and the rank only
+// when the caller writes it.
+__device__ __forceinline__ void resolve_round0(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b) {
     BlockInfo B = a.blk[b];
-    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
-        return;
+    if (!KGB_OK(id < a.cap_n && p < B.n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK)) return;
+    if (isa_nxt) isa_nxt[id] = p;
     a.L[(u64)B.off + b + p + 1] = id == B.off ? 0 : __ldg(a.T + id - 1);
     if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
-    res.eid[ridx] = id;
-    res.ekey[ridx] = p;
 }
 __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, ListView res,
                                         u32 ridx) {

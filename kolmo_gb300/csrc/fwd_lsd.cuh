@@ -81,7 +81,9 @@ __global__ void k_lsd_begin(FwdArgs a) {
     if (blockIdx.x == 0) {
         if (threadIdx.x < NSLOT) a.ltile[threadIdx.x] = 0;
         if (threadIdx.x == 0) {
-            c->cnt[L_R0 + c->rpar] = 0;
+            // round 0 lists no finished suffixes: with every id counted as finished, round 1's fixup copies the
+            // whole rank buffer
+            c->cnt[L_R0 + c->rpar] = a.idn;
             c->lsd_act = 0;
             c->m = a.blk[a.B - 1].soff + a.blk[a.B - 1].n;
         }
@@ -512,8 +514,8 @@ __device__ __forceinline__ u64 block_excl_sum64(u64 v, u64 *ws, u64 *total) {
     return before + inc - v;
 }
 
-// Emit, part 1 (group ends): groups of one resolve (rank unless k_seg_rank writes the ranks, L column, resolved
-// list); every other group takes its slots in the next tiny-group list
+// Emit, part 1 (group ends): groups of one resolve (rank unless k_seg_rank writes the ranks, L column); every other
+// group takes its slots in the next tiny-group list
 // (<= GTINY), medium-group list (<= GMED), small-group list (<= SMAX) or large-group list, writes its descriptor (and
 // tile-map entries), and records its slot base and index at its first position for part 2. Slots are allocated once
 // per tile (a count pass, a block scan, one atomic per list).
@@ -526,7 +528,6 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
     const u32 rpar = c->rpar, round = c->round;
     const ListView sl = a.lists[L_S0 + (rpar ^ 1)], ll = a.lists[L_L0 + (rpar ^ 1)], tl_ = a.lists[L_P0 + (rpar ^ 1)];
     const ListView ml_ = a.lists[L_M0 + (rpar ^ 1)];
-    const ListView res = a.lists[L_R0 + rpar];
     const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 TS = a.smax;
     for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -562,12 +563,10 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
             } else {
                 base[3] = 0;
             }
-            base[0] = (ts & 0xFFFF) ? atomicAdd(&c->cnt[L_R0 + rpar], ts & 0xFFFF) : 0ull;
             base[1] = (ts >> 16) & 0xFFFF ? atomicAdd(&c->cnt[L_S0 + (rpar ^ 1)], (((ts >> 16) & 0xFFFF) << 32) | (ts >> 32)) : 0ull;
             base[2] = (u32)tl ? atomicAdd(&c->cnt[L_L0 + (rpar ^ 1)], (tl << 32) | (tl >> 32)) : 0ull;
         }
         __syncthreads();
-        u32 r1 = (u32)base[0] + (u32)(xs & 0xFFFF);
         u32 sidx = (u32)(base[1] >> 32) + (u32)((xs >> 16) & 0xFFFF), se = (u32)base[1] + (u32)(xs >> 32);
         u32 lidx = (u32)(base[2] >> 32) + (u32)xl, le = (u32)base[2] + (u32)(xl >> 32);
         u32 tidx = (u32)(base[3] >> 32) + (u32)xt, te = (u32)base[3] + (u32)(xt >> 32);
@@ -598,8 +597,7 @@ __global__ void __launch_bounds__(TPB) k_seg_emit1(FwdArgs a) {
                 const u32 b = bv[q];
                 const u32 head = gf - a.blk[b].soff;
                 if (len == 1) {
-                    if (!a.rank_passes && idv[q] < a.cap_n) a.isa[rpar ^ 1][idv[q]] = head;
-                    resolve_norank(a, idv[q], head, b, res, r1++);
+                    resolve_round0(a, a.rank_passes ? nullptr : a.isa[rpar ^ 1], idv[q], head, b);
                     continue;
                 }
                 Seg g;
