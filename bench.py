@@ -1,10 +1,14 @@
-"""Benchmark of the GPU BWT path: one step = forward BWT + inverse BWT of one block.
+"""Benchmark of the GPU BWT path: one step = forward BWT + inverse BWT of the workload's blocks.
 
 Default workload (the single-block configuration): a 64 MiB block of Zipf(1.1) word-token prose (50k-word
 vocabulary, 2% random bytes, 200 verbatim 4-64 KiB repeats), seeded synthetic data standing in for the reference's
-text corpora. The codec-18 sampling interval for the block (2^23, 7 samples) is used.
+text corpora. The codec-18 sampling interval for the block (2^23, 7 samples) is used. Other workloads:
+markov1 (one 1 MiB order-2 Markov block), degenerate (four 128 MiB blocks: periodic 1 / 7 / 4096 with a flip per
+MiB, the Fibonacci word), batch (256 mixed blocks of 16 KiB-16 MiB), slices (the -9 planner's 128 trial slices of
+512 KiB) and serve (Poisson compress/decompress requests on the request server).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload prose64|batch]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload prose64|markov1|degenerate|batch|slices|serve]
 
 Output: one JSON line on rank 0.
   value   MiB/s of forward+inverse with the input resident in HBM, timed with CUDA events on the engine's stream,
@@ -14,9 +18,11 @@ Output: one JSON line on rank 0.
           pinned host buffers, host<->device copies inside the timed region;
   roofline   the dominant kernel (largest share of device time in a profiled pass of one step, CUDA events around
           every launch of the plain path on the same stream) against the measured HBM copy bandwidth;
-  cpu_baseline  the CPU sorter timed on this host's cores on a bounded sample of the same workload.
---impl reference times the reference's own CPU sorter (built from its sources where the reference tree was present,
-else the CPU restatement in oracle/) on the same workload.
+  cpu_baseline  the reference's own CPU sorter (compiled on this host from the reference's sources by
+          oracle/Makefile) on the whole workload with all host threads, and with one ("t1"); where it is not
+          available, the CPU restatement in oracle/ on a bounded sample.
+--impl reference times the reference's own CPU sorter (else the restatement) on the same workload, each step the
+whole workload, with all host threads.
 """
 from __future__ import annotations
 
@@ -146,13 +152,14 @@ class Clocks:
 
 
 # ------------------------------------------------------------------------------------------------ CPU sorter
-def cpu_sorter():
-    """(kind, callable fwd(T, r) -> (rc, U, I), inv(U, r, I) -> (rc, T), threads): the reference's own sorter when
-    it was built on a machine like this one and loads here, else the CPU restatement."""
+def cpu_sorter(threads: int | None = None):
+    """(kind, fwd(T, r) -> (rc, U, I), inv(U, r, I) -> (rc, T), threads): the reference's own sorter
+    (kolmo_sais_bwt_aux / kolmo_sais_unbwt_aux, src/algo/sais/sais.c:12027-12082, compiled on this machine from the
+    reference's sources by oracle/Makefile) when it loads here, else the CPU restatement."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     if O.ref_lib() is not None:
         return ("reference", lambda T, r: O.bwt_aux(T, r, use_ref=True, threads=threads),
                 lambda U, r, I: O.unbwt_aux(U, r, I, use_ref=True, threads=threads), threads)
@@ -161,9 +168,9 @@ def cpu_sorter():
     return ("port", lambda T, r: O.bwt_aux(T, r), lambda U, r, I: O.unbwt_aux(U, r, I, threads=threads), threads)
 
 
-def time_cpu(T: np.ndarray, r: int, budget_s: float, max_reps: int = 3):
+def time_cpu(T: np.ndarray, r: int, budget_s: float, max_reps: int = 3, threads: int | None = None):
     """fwd+inv MiB/s of the CPU sorter on T (repeated while the budget allows)."""
-    kind, fwd, inv, threads = cpu_sorter()
+    kind, fwd, inv, threads = cpu_sorter(threads)
     reps, total = 0, 0.0
     while reps < max_reps:
         t0 = time.perf_counter()
@@ -177,6 +184,38 @@ def time_cpu(T: np.ndarray, r: int, budget_s: float, max_reps: int = 3):
     return kind, threads, reps * T.size / MIB / total, reps
 
 
+def cpu_baseline(blocks: list, budget_s: float = 30.0) -> dict:
+    """The CPU sorter on this host: the reference's own sorter on the whole workload with all host threads and with
+    one (the reference's -T N and -T 1), else the restatement on a bounded sample of the first block."""
+    from kolmo_gb300.host import codec18_rlog
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    nproc = os.cpu_count() or 1
+    if O.ref_lib() is not None:
+        res = {}
+        for t in (nproc, 1):
+            tot, nbytes = 0.0, 0
+            for T in blocks:
+                r = 1 << codec18_rlog(T.size)
+                _, _, v, _ = time_cpu(T, r, budget_s=0.0, max_reps=1, threads=t)
+                tot += T.size / MIB / v
+                nbytes += T.size
+            res[t] = nbytes / MIB / tot
+        return {"value": round(res[nproc], 2), "unit": "MiB/s", "cores": nproc, "kind": "reference",
+                "sample": f"the whole workload ({sum(T.size for T in blocks) / MIB:.0f} MiB), forward+inverse, "
+                          f"kolmo_sais_bwt_aux + kolmo_sais_unbwt_aux with threads={nproc}",
+                "t1": {"value": round(res[1], 2), "cores": 1}}
+    T = blocks[0]
+    r = 1 << codec18_rlog(T.size)
+    sample = T[: min(T.size, 16 * MIB)]
+    kind, threads, v, reps = time_cpu(sample, r, budget_s=12.0)
+    return {"value": round(v, 2), "unit": "MiB/s", "cores": threads, "kind": kind,
+            "sample": f"first {sample.size / MIB:.0f} MiB of the first block, forward+inverse, {reps} run(s), r={r}; "
+                      "forward on one thread, inverse on all"}
+
+
 # ------------------------------------------------------------------------------------------------ workloads
 def prose_block(rank: int, mib: int = 64):
     from kolmo_gb300 import workloads as W
@@ -186,37 +225,80 @@ def prose_block(rank: int, mib: int = 64):
     return W.zipf_prose(mib * MIB, W.SEED_PROSE_64MIB + rank)
 
 
+DEGENERATE_KINDS = ("periodic-1", "periodic-7", "periodic-4096", "fibonacci")
+
+
+def single_blocks(workload: str, rank: int, mib: int):
+    """The blocks of a single-block workload (each block is its own forward and inverse call, as the drop-in path
+    runs them) and its description."""
+    from kolmo_gb300 import workloads as W
+
+    if workload == "markov1":
+        return [("markov1", W.markov_1mib())], ("markov1: one 1 MiB order-2 Markov block (64 symbols, Dirichlet 0.3 "
+                                                "rows), forward + inverse BWT")
+    if workload == "degenerate":
+        return ([(k, W.degenerate(k)) for k in DEGENERATE_KINDS],
+                "degenerate: four 128 MiB blocks (periodic with periods 1, 7 and 4096 and one random flip per MiB; "
+                "the Fibonacci word), each forward + inverse BWT")
+    return [("prose64", prose_block(rank, mib))], (f"prose64: one {mib} MiB Zipf(1.1) word-token prose block per GPU, "
+                                                   "forward + inverse BWT")
+
+
 # DRAM bytes per unit (suffix) measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the 16 MiB prose
 # case: profiles/traffic_group_thread_lsd_pass_prose16.md (tiny groups) and profiles/lsd_pass_prose16.md (the
 # round-0 radix pass, averaged over a 16-pass step). The 64 MiB launch's traffic is scaled by the suffixes it
 # processes.
 TRAFFIC_PER_SUFFIX = {"group_thread": 35.1, "lsd_pass": 13.9}
+RANK_SORTERS = ("tile_sort_rank", "tile_warp_rank", "group_thread", "group_warp", "keygen")
 
 
-def algorithmic_bytes(rec: dict) -> float:
-    """Algorithmic bytes of one launch (the per-unit figures of the doubling model): a rank round costs 48 B per
-    active suffix (read its id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id),
-    a round-0 radix pass 16 B per suffix (read and write its 8 B item: id and one 4-byte key group), the inverse 10 B
-    per byte over its passes (psi build: read L, write psi; walk: read psi, write text)."""
+def algorithmic_bytes(rec: dict, round0_launches: int, round0_elems: int) -> float:
+    """Algorithmic bytes of one launch, by the doubling model's per-unit figures: round 0 (the sort of every suffix
+    by its first W bytes) costs 33 B per suffix in all, credited in equal parts to its radix passes (or, on the tile
+    path, to its prefix tile kernels by the suffixes they sort); rank round j costs 48 B per active suffix (read its
+    id, gather two ranks, read+write a 12 B (key, id) pair, write SA, rank and compacted id), credited to the kernel
+    that sorts the suffix (the large list's suffixes once, at their key generation); the inverse 10 B per byte (psi
+    build: read L, write psi; walk: read psi, write text). Scans, segmentation, bucket passes and fixups are
+    overhead in the model and get no bytes."""
     k, e = rec["kernel"], rec["elems"]
-    if k in ("tile_sort_rank", "tile_sort_rank_keyed", "tile_warp_rank", "tile_warp_rank_keyed", "group_thread",
-             "group_warp"):
+    if k in RANK_SORTERS:
         return 48.0 * e
     if k == "lsd_pass":
-        return 16.0 * e  # every pass reads and writes each suffix's 8 B item
-    if k in ("tile_sort_prefix", "tile_sort_prefix_keyed", "tile_warp_prefix", "tile_warp_prefix_keyed"):
+        return 33.0 * round0_elems / max(round0_launches, 1)
+    if k in ("tile_sort_prefix", "tile_warp_prefix"):
         return 33.0 * e
-    if k == "inv_walk":
-        return 5.0 * e   # read psi 4 B + write 1 B per decoded byte
-    if k == "inv_scatter":
-        return 5.0 * e   # read L 1 B + write psi 4 B per byte
-    if k in ("msd_hist",):
-        return 8.0 * e
-    if k in ("msd_scatter",):
-        return 16.0 * e
-    if k == "keygen":
-        return 12.0 * e
+    if k in ("inv_walk", "inv_scatter"):
+        return 5.0 * e
     return 0.0
+
+
+def profile_table(prof_f: list, prof_i: list, n: int, h0: int, peak: float) -> tuple:
+    """Per-kernel totals with algorithmic bytes, and the per-round table (m_j, h, time, GB/s and fraction of peak)."""
+    r0 = [rec for rec in prof_f if rec["round"] == 0 and rec["kernel"] == "lsd_pass"]
+    by_kernel = {}
+    for rec in prof_f + prof_i:
+        d = by_kernel.setdefault(rec["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0.0, "elems": 0})
+        d["launches"] += 1
+        d["ms"] += rec["ms"]
+        d["elems"] += rec["elems"]
+        d["bytes"] += algorithmic_bytes(rec, len(r0), n)
+    rounds = {}
+    for rec in prof_f:
+        rr = rounds.setdefault(rec["round"], {"ms": 0.0, "m": 0})
+        rr["ms"] += rec["ms"]
+        # active suffixes of a rank round: the small, tiny and medium lists (their sort kernels) and the large list
+        # (keygen); the keyed tiles sort buckets of the large list and are not counted again
+        if rec["kernel"] in RANK_SORTERS:
+            rr["m"] += rec["elems"]
+    table = []
+    for j in sorted(rounds):
+        m = rounds[j]["m"] if j > 0 else n
+        b = (48.0 if j > 0 else 33.0) * m
+        ms = rounds[j]["ms"]
+        gbs = b / (ms / 1e3) / 1e9 if ms > 0 else None
+        table.append({"round": j, "h": 0 if j == 0 else h0 << (j - 1), "m": m, "ms": round(ms, 4),
+                      "GBs": round(gbs, 1) if gbs else None, "frac": round(gbs / peak, 4) if gbs else None})
+    return by_kernel, table
 
 
 def run_ours(args, world, rank, local):
@@ -227,24 +309,36 @@ def run_ours(args, world, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    T = prose_block(rank, args.block_mib)
-    n = int(T.size)
-    r = 1 << codec18_rlog(n)
-    ns = n_samples(n, r)
+    named, wname = single_blocks(args.workload, rank, args.block_mib)
+    nmax = max(int(T.size) for _, T in named)
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
     eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0,
                args.lsd_bytes)
-    dT = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
-    dT[:n] = torch.from_numpy(T).to(dev)
-    dL = torch.zeros(n + 1, dtype=torch.uint8, device=dev)
-    dI = torch.zeros(ns, dtype=torch.int32, device=dev)
-    dU = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
-    dOut = torch.zeros(n + 64, dtype=torch.uint8, device=dev)
+    dT = torch.zeros(nmax + 64, dtype=torch.uint8, device=dev)
+    dL = torch.zeros(nmax + 1, dtype=torch.uint8, device=dev)
+    dI = torch.zeros(n_samples(nmax, 2), dtype=torch.int32, device=dev)
+    dU = torch.zeros(nmax + 64, dtype=torch.uint8, device=dev)
+    dOut = torch.zeros(nmax + 64, dtype=torch.uint8, device=dev)
+    # the text of every block stays resident; a step copies none of it from the host
+    resident = [torch.from_numpy(T).to(dev) for _, T in named]
     flush = torch.empty(256 * MIB, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
+    total = sum(int(T.size) for _, T in named)
 
-    def step(plain=False):
+    def load(b):
+        """puts block b's resident text into the engine's input buffer (outside the timed region)"""
+        n = int(named[b][1].size)
+        with torch.cuda.stream(s):
+            dT[:n].copy_(resident[b])
+            dT[n:n + 64].zero_()
+
+    def one_block(b, plain=False):
+        """forward + inverse of block b (already in dT); returns (fwd ms, inv ms) from CUDA events on the engine
+        stream."""
+        T = named[b][1]
+        n = int(T.size)
+        r = 1 << codec18_rlog(n)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         ev[0].record(s)
         rc = eng.fwd(dT, dL, dI, [(0, n, r, 0)], stream=s, plain=plain)
@@ -262,117 +356,126 @@ def run_ours(args, world, rank, local):
         rc2, st = eng.wait(1)
         if rc or rc2:
             raise RuntimeError(f"inverse failed: {rc} {rc2} {native.last_error()}")
-        return ev
+        s.synchronize()
+        return ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
 
     # warm-up (also the correctness check of this run)
+    load(0)
     for _ in range(max(args.warmup, 1)):
-        step(plain=args.plain)
-    s.synchronize()
-    assert torch.equal(dOut[:n], dT[:n]), "round trip failed"
-    if rank == 0:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        for b in range(len(named)):
+            if len(named) > 1:
+                load(b)
+            one_block(b, plain=args.plain)
+            assert torch.equal(dOut[:named[b][1].size], resident[b]), f"round trip failed: {named[b][0]}"
 
     clocks = Clocks(local)
     barrier(world)
     torch.cuda.synchronize()
     clocks.start()
     times, tf, ti = [], [], []
+    per_block = [[0.0, 0.0] for _ in named]
     for _ in range(args.steps):
-        with torch.cuda.stream(s):
-            flush.fill_(1)
-        ev = step(plain=args.plain)
-        s.synchronize()
-        tf.append(ev[0].elapsed_time(ev[1]))
-        ti.append(ev[2].elapsed_time(ev[3]))
-        times.append(ev[0].elapsed_time(ev[3]))
+        step = 0.0
+        for b in range(len(named)):
+            if len(named) > 1:
+                load(b)
+            with torch.cuda.stream(s):
+                flush.fill_(1)
+            f_ms, i_ms = one_block(b, plain=args.plain)
+            tf.append(f_ms)
+            ti.append(i_ms)
+            per_block[b][0] += f_ms
+            per_block[b][1] += i_ms
+            step += f_ms + i_ms
+        times.append(step)
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(world)
     total_ms = reduce_max(sum(times), world, dev)
-    value = world * args.steps * n / MIB / (total_ms / 1e3)
+    value = world * args.steps * total / MIB / (total_ms / 1e3)
     if args.skip_extras:  # timed steps only (profiler runs)
         return {"metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
-                "fwd_ms": round(sum(tf) / len(tf), 3), "inv_ms": round(sum(ti) / len(ti), 3),
-                "block_bytes": n, "skip_extras": True,
+                "fwd_ms": round(sum(tf) / args.steps, 3), "inv_ms": round(sum(ti) / args.steps, 3),
+                "bytes": total, "skip_extras": True,
                 "cfg": [args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path,
                         args.lsd_round0, args.lsd_bytes]}
 
-    # profiled pass (plain path, CUDA events around every launch on stream s)
-    eng.profile(True)
-    assert eng.fwd(dT, dL, dI, [(0, n, r, 0)], stream=s, plain=True) == 0 and eng.wait()[0] == 0
-    prof_f = eng.profile_read()
-    p0 = int(dI[0].item())
-    assert eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True) == 0 and eng.wait(1)[0] == 0
-    prof_i = eng.profile_read()
-    eng.profile(False)
-    if args.profile_out and rank == 0:
-        with open(args.profile_out, "w") as f:
-            json.dump({"forward": prof_f, "inverse": prof_i}, f)
-    launches_fwd = sum(1 for x in prof_f)
-    launches_inv = sum(1 for x in prof_i)
-    prof = prof_f + prof_i
-    by_kernel = {}
-    for rec in prof:
-        d = by_kernel.setdefault(rec["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0.0})
-        d["launches"] += 1
-        d["ms"] += rec["ms"]
-        d["bytes"] += algorithmic_bytes(rec)
+    # profiled pass (plain path, CUDA events around every launch on stream s), one per block
+    peak, peak_kind = peaks()
+    by_kernel, blocks_out = {}, []
+    launches = 0
+    for b, (name, T) in enumerate(named):
+        n = int(T.size)
+        r = 1 << codec18_rlog(n)
+        load(b)
+        eng.profile(True)
+        assert eng.fwd(dT, dL, dI, [(0, n, r, 0)], stream=s, plain=True) == 0 and eng.wait()[0] == 0
+        prof_f = eng.profile_read()
+        p0 = int(dI[0].item())
+        with torch.cuda.stream(s):
+            dU[:p0].copy_(dL[:p0])
+            dU[p0:n].copy_(dL[p0 + 1:n + 1])
+        assert eng.inv(dU, dOut, [(0, n, p0)], stream=s, plain=True) == 0 and eng.wait(1)[0] == 0
+        prof_i = eng.profile_read()
+        eng.profile(False)
+        if args.profile_out and rank == 0:
+            with open(args.profile_out if len(named) == 1 else f"{args.profile_out}.{name}", "w") as f:
+                json.dump({"forward": prof_f, "inverse": prof_i}, f)
+        launches += len(prof_f) + len(prof_i)
+        lc = eng.last_config()
+        h0 = lc["lsd_bytes"] if lc["lsd_round0"] else 8  # prefix bytes round 0 sorts (the first rank round's h)
+        bk, table = profile_table(prof_f, prof_i, n, h0, peak)
+        for k, d in bk.items():
+            a = by_kernel.setdefault(k, {"launches": 0, "ms": 0.0, "bytes": 0.0, "elems": 0})
+            for f in a:
+                a[f] += d[f]
+        blocks_out.append({"block": name, "bytes": n, "r": r, "fwd_ms": round(per_block[b][0] / args.steps, 3),
+                           "inv_ms": round(per_block[b][1] / args.steps, 3), "rounds": table})
     tot_ms = sum(d["ms"] for d in by_kernel.values())
     dom = max((k for k in by_kernel if k != "control"), key=lambda k: by_kernel[k]["ms"])
     dd = by_kernel[dom]
-    peak, peak_kind = peaks()
-    achieved = dd["bytes"] / dd["launches"] / (dd["ms"] / dd["launches"] / 1e3) / 1e9 if dd["ms"] > 0 else 0.0
-    rounds = {}
-    for rec in prof_f:
-        rr = rounds.setdefault(rec["round"], {"ms": 0.0, "m": 0})
-        rr["ms"] += rec["ms"]
-        # active suffixes of a rank round: the small, tiny and medium lists (their sort kernels) and the large list
-        # (keygen); the keyed tiles sort buckets of the large list and are not counted again
-        if rec["kernel"] in ("tile_sort_rank", "tile_warp_rank", "group_thread", "group_warp", "keygen"):
-            rr["m"] += rec["elems"]
-    round_table = []
-    lc = eng.last_config()
-    h0 = lc["lsd_bytes"] if lc["lsd_round0"] else 8  # prefix bytes round 0 sorts (the first rank round's h)
-    for j in sorted(rounds):
-        m = rounds[j]["m"] if j > 0 else n
-        b = (48.0 if j > 0 else 33.0) * m
-        ms = rounds[j]["ms"]
-        round_table.append({"round": j, "h": 0 if j == 0 else h0 << (j - 1), "m": m, "ms": round(ms, 4),
-                            "GBs": round(b / (ms / 1e3) / 1e9, 1) if ms > 0 else None})
+    achieved = dd["bytes"] / (dd["ms"] / 1e3) / 1e9 if dd["ms"] > 0 else 0.0
 
     # e2e through the drop-in C ABI with pinned host buffers
-    e2e = run_e2e(T, r, args.steps, max(args.warmup, 1), world, dev)
+    e2e = run_e2e([T for _, T in named], args.steps, max(args.warmup, 1), world, dev)
 
+    cfg = {"workload": wname, "bytes": total, "blocks": [{"block": nm, "bytes": int(T.size),
+                                                          "r": 1 << codec18_rlog(int(T.size))} for nm, T in named],
+           "l2": "flushed before every block (256 MiB write)", "parallelism": f"replicas{world}", "tile_cap": 4096}
     out = {
         "metric": "bwt_fwd_inv_MiB_per_s", "value": round(value, 2), "unit": "MiB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "prose64: one 64 MiB Zipf(1.1) word-token prose block per GPU, forward + inverse BWT",
-                   "block_bytes": n, "r": r, "samples": ns, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas{world}", "tile_cap": 4096},
-        "fwd_MiB_per_s": round(args.steps * n / MIB / (sum(tf) / 1e3), 2),
-        "inv_MiB_per_s": round(args.steps * n / MIB / (sum(ti) / 1e3), 2),
+        "config": cfg,
+        "fwd_MiB_per_s": round(args.steps * total / MIB / (sum(tf) / 1e3), 2),
+        "inv_MiB_per_s": round(args.steps * total / MIB / (sum(ti) / 1e3), 2),
         "e2e": e2e,
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                      "launches_per_step": dd["launches"], "share": round(dd["ms"] / tot_ms, 4),
-                     "bytes_model": "rank round 48 B per active suffix, round-0 radix pass 16 B per suffix (per "
-                                    "launch: elements of the launch's work list)"},
+                     "bytes_model": "doubling model: round 0 33 B per suffix over its radix passes, rank round 48 B "
+                                    "per active suffix, inverse 10 B per byte; scans, segmentation, bucket passes "
+                                    "and fixups get none"},
         "kernel_shares": {k: round(v["ms"] / tot_ms, 4) for k, v in sorted(by_kernel.items(), key=lambda x: -x[1]["ms"])},
-        "rounds": round_table,
-        "gpu_launches": args.steps * (launches_fwd + launches_inv),
+        "gpu_launches": args.steps * launches,
         "clocks": clk,
     }
+    if len(blocks_out) == 1:
+        out["rounds"] = blocks_out[0]["rounds"]
+    else:
+        out["blocks"] = blocks_out
+    if dom == "lsd_pass":
+        # the pass itself: every pass reads and writes each suffix's 8-byte item (id and one 4-byte key group)
+        item = 16.0 * dd["elems"] / (dd["ms"] / 1e3) / 1e9
+        out["roofline"]["item_traffic"] = {"achieved": round(item, 1), "frac": round(item / peak, 4),
+                                           "model": "16 B per suffix per radix pass (read and write its item)"}
     if dom in TRAFFIC_PER_SUFFIX:
-        elems = sum(rec["elems"] for rec in prof if rec["kernel"] == dom) / max(dd["launches"], 1)
+        elems = dd["elems"] / max(dd["launches"], 1)
         out["roofline"]["traffic"] = round(TRAFFIC_PER_SUFFIX[dom] * elems)
         out["roofline"]["traffic_source"] = "ncu dram bytes per suffix on the 16 MiB case x suffixes per launch"
     if rank == 0:
-        kind, threads, cpu_v, reps = time_cpu(T[: 16 * MIB], r, budget_s=12.0)
-        out["cpu_baseline"] = {"value": round(cpu_v, 2), "unit": "MiB/s", "cores": threads, "kind": kind,
-                               "sample": f"first 16 MiB of the block, forward+inverse, {reps} run(s), r={r}"
-                                         + ("; forward on one thread, inverse on all" if kind == "port" else "")}
+        out["cpu_baseline"] = cpu_baseline([T for _, T in named])
     return out
 
 
@@ -655,30 +758,36 @@ def run_serve(args, world, rank, local):
     }
 
 
-def run_e2e(T, r, steps, warmup, world, dev):
+def run_e2e(texts: list, steps: int, warmup: int, world: int, dev):
+    """The workload through the drop-in C ABI (kolmo_sais_bwt_aux, then kolmo_sais_unbwt_aux on its output) from
+    pinned host buffers; every step copies each block's text in and its BWT and decoded text out."""
     import torch
 
     from kolmo_gb300 import native
-    from kolmo_gb300.host import n_samples
+    from kolmo_gb300.host import codec18_rlog, n_samples
 
     L = native.lib()
-    n = int(T.size)
-    Th = torch.from_numpy(T.copy()).pin_memory()
-    Uh = torch.empty(n, dtype=torch.uint8).pin_memory()
-    Bh = torch.empty(n, dtype=torch.uint8).pin_memory()
-    I = np.zeros(n_samples(n, r), np.int32)
     A = np.zeros(1, np.int32)
-    tp, up, bp = Th.data_ptr(), Uh.data_ptr(), Bh.data_ptr()
+    bufs = []
+    for T in texts:
+        n = int(T.size)
+        r = 1 << codec18_rlog(n)
+        Th = torch.from_numpy(T.copy()).pin_memory()
+        Uh = torch.empty(n, dtype=torch.uint8).pin_memory()
+        Bh = torch.empty(n, dtype=torch.uint8).pin_memory()
+        bufs.append((n, r, Th, Uh, Bh, np.zeros(n_samples(n, r), np.int32)))
 
     def one():
-        rc = L.kolmo_sais_bwt_aux(tp, up, A.ctypes.data, n, r, I.ctypes.data, 1)
-        rc2 = L.kolmo_sais_unbwt_aux(up, bp, A.ctypes.data, n, r, I.ctypes.data, 1)
-        if rc or rc2:
-            raise RuntimeError(f"C ABI round trip failed: {rc} {rc2} {native.last_error()}")
+        for n, r, Th, Uh, Bh, I in bufs:
+            rc = L.kolmo_sais_bwt_aux(Th.data_ptr(), Uh.data_ptr(), A.ctypes.data, n, r, I.ctypes.data, 1)
+            rc2 = L.kolmo_sais_unbwt_aux(Uh.data_ptr(), Bh.data_ptr(), A.ctypes.data, n, r, I.ctypes.data, 1)
+            if rc or rc2:
+                raise RuntimeError(f"C ABI round trip failed: {rc} {rc2} {native.last_error()}")
 
     for _ in range(warmup):
         one()
-    assert torch.equal(Bh, Th), "C ABI round trip differs"
+    for n, r, Th, Uh, Bh, I in bufs:
+        assert torch.equal(Bh, Th), "C ABI round trip differs"
     barrier(world)
     t = 0.0
     for _ in range(steps):
@@ -686,47 +795,62 @@ def run_e2e(T, r, steps, warmup, world, dev):
         one()
         t += time.perf_counter() - t0
     t = reduce_max(t, world, dev)
-    return {"value": round(world * steps * n / MIB / t, 2), "unit": "MiB/s", "h2d_bytes_per_step": 2 * n,
-            "d2h_bytes_per_step": (n + 1) + 4 * int(I.size) + n,
+    total = sum(b[0] for b in bufs)
+    return {"value": round(world * steps * total / MIB / t, 2), "unit": "MiB/s", "h2d_bytes_per_step": 2 * total,
+            "d2h_bytes_per_step": 2 * total + sum(4 * int(b[5].size) for b in bufs),
             "path": "kolmo_sais_bwt_aux + kolmo_sais_unbwt_aux, pinned host buffers"}
 
 
 def run_reference(args, world, rank):
+    """The reference's own CPU sorter on the same workload, on this host's cores: kolmo_sais_bwt_aux and
+    kolmo_sais_unbwt_aux compiled from the reference's sources (oracle/Makefile) with every host thread, each step the
+    whole workload. Where that library is not available the CPU restatement runs on a bounded sample instead."""
     if rank != 0:
         return None
-    T = prose_block(0)
     from kolmo_gb300.host import codec18_rlog
 
-    r = 1 << codec18_rlog(T.size)
+    named, wname = single_blocks(args.workload if args.workload in ("markov1", "degenerate") else "prose64", 0,
+                                 args.block_mib)
+    texts = [T for _, T in named]
     kind, fwd, inv, threads = cpu_sorter()
-    # size the per-step sample so that warm-up + steps stay within about two minutes
-    probe = T[: 4 * MIB]
-    t0 = time.perf_counter()
-    rc, U, I = fwd(probe, r)
-    inv(U, r, I)
-    speed = probe.size / (time.perf_counter() - t0)  # bytes/s
-    per_step = 120.0 / max(args.steps + args.warmup, 1)
-    sample = int(min(T.size, max(4 * MIB, speed * per_step)))
-    S = T[:sample]
+    if kind == "reference":
+        samples = texts
+        desc = (f"the whole workload ({sum(T.size for T in texts) / MIB:.0f} MiB) per step, forward+inverse, "
+                f"kolmo_sais_bwt_aux + kolmo_sais_unbwt_aux with threads={threads}")
+    else:
+        # size the per-step sample so that warm-up + steps stay within about two minutes
+        T = texts[0]
+        r = 1 << codec18_rlog(T.size)
+        probe = T[: 4 * MIB]
+        t0 = time.perf_counter()
+        rc, U, I = fwd(probe, r)
+        inv(U, r, I)
+        speed = probe.size / (time.perf_counter() - t0)  # bytes/s
+        per_step = 120.0 / max(args.steps + args.warmup, 1)
+        samples = [T[: int(min(T.size, max(4 * MIB, speed * per_step)))]]
+        desc = (f"first {samples[0].size / MIB:.1f} MiB of the first block per step, forward+inverse, r={r}; "
+                f"forward on one thread (SA-IS restatement), inverse on {threads} threads (per-sample decode)")
+    rs = [1 << codec18_rlog(S.size) for S in samples]
     for _ in range(args.warmup):
-        fwd(S, r)
+        for S, r in zip(samples, rs):
+            fwd(S, r)
     t = 0.0
     for _ in range(args.steps):
-        t0 = time.perf_counter()
-        rc, U, I = fwd(S, r)
-        rc2, back = inv(U, r, I)
-        t += time.perf_counter() - t0
-        assert rc == 0 and rc2 == 0
-    v = args.steps * sample / MIB / t
-    desc = f"first {sample / MIB:.1f} MiB of the 64 MiB prose block per step, forward+inverse, r={r}"
-    if kind == "port":
-        desc += f"; forward on one thread (SA-IS restatement), inverse on {threads} threads (per-sample decode)"
+        for S, r in zip(samples, rs):
+            t0 = time.perf_counter()
+            rc, U, I = fwd(S, r)
+            rc2, back = inv(U, r, I)
+            t += time.perf_counter() - t0
+            assert rc == 0 and rc2 == 0
+    total = sum(S.size for S in samples)
+    v = args.steps * total / MIB / t
     return {"metric": "bwt_fwd_inv_MiB_per_s", "value": round(v, 2), "unit": "MiB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "prose64: one 64 MiB Zipf(1.1) word-token prose block, forward + inverse BWT",
-                       "block_bytes": int(T.size), "r": r, "parallelism": "cpu"},
+            "config": {"workload": wname, "bytes": int(sum(T.size for T in texts)),
+                       "blocks": [{"block": nm, "bytes": int(T.size), "r": 1 << codec18_rlog(int(T.size))}
+                                  for nm, T in named], "parallelism": "cpu", "same_config": kind == "reference"},
             "cpu_baseline": {"value": round(v, 2), "unit": "MiB/s", "cores": threads, "kind": kind, "sample": desc},
             "e2e": {"value": round(v, 2), "unit": "MiB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -737,7 +861,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="prose64", choices=["prose64", "batch", "slices", "serve"])
+    ap.add_argument("--workload", default="prose64",
+                    choices=["prose64", "markov1", "degenerate", "batch", "slices", "serve"])
     ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests per second)")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
     ap.add_argument("--slots", type=int, default=3, help="serve: server workers")

@@ -7,7 +7,8 @@
  *    checks it like the reference does and does not touch it. `threads` is accepted and ignored (the output never
  *    depends on it, as in the reference). Returns 0, -1 for bad arguments or indexes out of range (for the inverse
  *    also: a string that is not a valid BWT), -2 when device memory or the device is unavailable. There is no CPU
- *    fallback. Calls from several threads are serialised on one device context.
+ *    fallback. Calls from several threads share one device worker: concurrent calls are coalesced into batches
+ *    (kgbwt_dropin_stats), and each call's result is the one it would get alone.
  * 2. Batch entry points: many blocks in one device pass (one CUDA-graph launch).
  * 3. Engine entry points: device-resident buffers on a caller stream, for servers that keep data on the GPU.
  */
@@ -196,6 +197,17 @@ int32_t kgbwt_server_plan(const int32_t *kinds, const int32_t *n, const int32_t 
                           uint64_t have_inv, uint64_t avail, uint64_t max_batch_bytes, int32_t *take);
 /* Device bytes a worker with no workspace needs for one batch of these requests (host only). */
 uint64_t kgbwt_estimate_bytes(int32_t kind, const int32_t *n, const int32_t *r, int32_t count);
+
+/* ---- coalescing of concurrent drop-in and batch calls -------------------------------------------------------------
+ * No counterpart in the reference, whose block workers each run their own CPU sort (src/core/blocks.c:181,
+ * src/core/compress.c:221, src/core/decode.c:405). Every call of sections 1 and 2 queues on the library's default
+ * worker; the first caller to find it idle runs the oldest pending call together with every later pending call of
+ * the same direction, in arrival order, while their input stays within KGBWT_BATCH_MIB (environment, default 256)
+ * MiB, and the other callers wait. If such a combined batch fails at the device level (-2), each of its calls is run
+ * again alone. With KGBWT_STATS=<path> in the environment every batch appends one line to that file.
+ * kgbwt_dropin_stats writes up to cap of: forward calls, forward batches, largest forward batch (calls), inverse
+ * calls, inverse batches, largest inverse batch, combined batches retried call by call; returns 7. */
+int32_t kgbwt_dropin_stats(int64_t *out, int32_t cap);
 
 /* ---- misc --------------------------------------------------------------------------------------------------------- */
 const char *kgbwt_last_error(void); /* text of the last error on this thread ("" if none) */

@@ -59,6 +59,14 @@ def unbwt(U, idx: int):
     return int(rc), out[:n]
 
 
+def dropin_stats() -> dict:
+    """Coalescing counters of the drop-in and batch calls (kgbwt_dropin_stats)."""
+    out = (ctypes.c_int64 * 7)()
+    native.lib().kgbwt_dropin_stats(ctypes.addressof(out), 7)
+    keys = ("fwd_calls", "fwd_batches", "fwd_largest", "inv_calls", "inv_batches", "inv_largest", "retried")
+    return dict(zip(keys, (int(x) for x in out)))
+
+
 def fwd_batch(blocks, plain: bool = False):
     """blocks: list of (T, r). Returns (rc, [(rc_i, U_i, I_i)])."""
     keep, jobs = [], (native.FwdJob * max(len(blocks), 1))()

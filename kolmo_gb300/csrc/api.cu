@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <condition_variable>
+#include <deque>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -68,14 +70,44 @@ Worker::~Worker() {
     if (stream) cudaStreamDestroy(stream);
 }
 
-// The default worker of the drop-in and batch calls, behind one lock.
+// One drop-in or batch call waiting for the default worker.
+struct Pending {
+    int kind;           // 0 forward, 1 inverse
+    void *jobs;         // kgbwt_fwd_job[count] or kgbwt_inv_job[count]
+    int32_t count;
+    uint32_t flags;
+    u64 bytes;          // input bytes of the call's jobs
+    int rc = 0;         // the device-level return code of the batch that carried the call
+    bool done = false;
+    char err[256] = {0};
+};
+
+// The default worker of the drop-in and batch calls. Concurrent callers (the reference's block workers call the
+// sorter from one thread per block, src/core/blocks.c:181, src/core/compress.c:221) are coalesced: the first caller
+// to find the worker idle runs the oldest pending call together with every later pending call of the same kind, in
+// arrival order, while their input stays within the batch cap; the others wait for their results.
 struct Context {
-    std::mutex mu;
+    std::mutex mu;  // guards the queue, `busy` and the counters; the worker itself belongs to the running leader
+    std::condition_variable cv;
+    std::deque<Pending *> q;
+    bool busy = false;
     Worker w;
+    int64_t calls[2] = {0, 0}, batches[2] = {0, 0}, largest[2] = {0, 0}, retried = 0;
 };
 static Context &ctx() {
     static Context *c = new Context();  // never destroyed: callers may run at process exit
     return *c;
+}
+
+// Input bytes per coalesced batch: KGBWT_BATCH_MIB (default 256 MiB, about 32 GB of forward workspace).
+static u64 batch_cap() {
+    static u64 cap = 0;
+    if (!cap) {
+        const char *e = getenv("KGBWT_BATCH_MIB");
+        const long v = e ? atol(e) : 0;
+        cap = (u64)(v > 0 ? v : 256) << 20;
+    }
+    return cap;
 }
 
 bool bad_r(int32_t r) { return r < 2 || (r & (r - 1)) != 0; }
@@ -350,15 +382,106 @@ bool tuned_config(u64 n, FwdConfig *out) {
     return true;
 }
 
-static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
+// KGBWT_STATS=<path>: every coalesced batch appends one line (kind, calls, jobs, input bytes, return code).
+static void log_batch(int kind, size_t calls, size_t jobs, u64 bytes, int rc) {
+    static const char *path = getenv("KGBWT_STATS");
+    if (!path || !*path) return;
+    if (FILE *f = fopen(path, "a")) {
+        fprintf(f, "%s calls=%zu jobs=%zu bytes=%llu rc=%d\n", kind ? "inv" : "fwd", calls, jobs,
+                (unsigned long long)bytes, rc);
+        fclose(f);
+    }
+}
+
+// Runs the calls `take` as one batch on the default worker (the caller is the leader and owns the worker).
+static void run_coalesced(Context &C, std::vector<Pending *> &take) {
+    const int kind = take[0]->kind;
+    const uint32_t flags = take[0]->flags;
+    size_t total = 0;
+    u64 bytes = 0;
+    for (Pending *p : take) { total += (size_t)p->count; bytes += p->bytes; }
+    int rc;
+    if (take.size() == 1) {
+        Pending *p = take[0];
+        rc = kind ? run_inv_jobs(C.w, (kgbwt_inv_job *)p->jobs, p->count, flags)
+                  : run_fwd_jobs(C.w, (kgbwt_fwd_job *)p->jobs, p->count, flags);
+        p->rc = rc;
+        if (rc) snprintf(p->err, sizeof p->err, "%s", g_err);
+    } else {
+        std::vector<kgbwt_fwd_job> fj;
+        std::vector<kgbwt_inv_job> ij;
+        for (Pending *p : take) {
+            if (kind) ij.insert(ij.end(), (kgbwt_inv_job *)p->jobs, (kgbwt_inv_job *)p->jobs + p->count);
+            else fj.insert(fj.end(), (kgbwt_fwd_job *)p->jobs, (kgbwt_fwd_job *)p->jobs + p->count);
+        }
+        rc = kind ? run_inv_jobs(C.w, ij.data(), (int32_t)ij.size(), flags)
+                  : run_fwd_jobs(C.w, fj.data(), (int32_t)fj.size(), flags);
+        if (rc == -2) {
+            // a device-level failure of the combined batch (out of memory, most likely): each call runs alone, so
+            // the result of a call never depends on what it was batched with
+            std::lock_guard<std::mutex> lock(C.mu);
+            C.retried++;
+        }
+        size_t k = 0;
+        for (Pending *p : take) {
+            if (rc == -2) {
+                p->rc = kind ? run_inv_jobs(C.w, (kgbwt_inv_job *)p->jobs, p->count, flags)
+                             : run_fwd_jobs(C.w, (kgbwt_fwd_job *)p->jobs, p->count, flags);
+            } else {
+                for (int32_t i = 0; i < p->count; i++, k++) {
+                    if (kind) ((kgbwt_inv_job *)p->jobs)[i].rc = ij[k].rc;
+                    else ((kgbwt_fwd_job *)p->jobs)[i].rc = fj[k].rc;
+                }
+                p->rc = rc;
+            }
+            if (p->rc) snprintf(p->err, sizeof p->err, "%s", g_err);
+        }
+    }
+    log_batch(kind, take.size(), total, bytes, rc);
+}
+
+// Queues one call and returns its device-level return code once a leader (possibly this thread) has run it.
+static int submit(Pending &p) {
     Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
-    return run_fwd_jobs(C.w, jobs, count, flags);
+    std::unique_lock<std::mutex> lk(C.mu);
+    C.q.push_back(&p);
+    C.calls[p.kind]++;
+    while (!p.done) {
+        if (C.busy) { C.cv.wait(lk); continue; }
+        C.busy = true;
+        std::vector<Pending *> take;
+        const Pending *first = C.q.front();
+        u64 bytes = 0;
+        for (auto it = C.q.begin(); it != C.q.end();) {
+            Pending *x = *it;
+            if (x->kind != first->kind || x->flags != first->flags) { ++it; continue; }
+            if (!take.empty() && bytes + x->bytes > batch_cap()) break;
+            take.push_back(x);
+            bytes += x->bytes;
+            it = C.q.erase(it);
+        }
+        lk.unlock();
+        run_coalesced(C, take);
+        lk.lock();
+        C.batches[take[0]->kind]++;
+        C.largest[take[0]->kind] = std::max<int64_t>(C.largest[take[0]->kind], (int64_t)take.size());
+        for (Pending *x : take) x->done = true;
+        C.busy = false;
+        C.cv.notify_all();
+    }
+    if (p.rc || p.err[0]) record_error(p.err);
+    return p.rc;
+}
+
+static int fwd_batch_impl(kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) {
+    Pending p{0, jobs, count, flags, 0};
+    for (int32_t i = 0; i < count; i++) p.bytes += jobs[i].n > 0 ? (u64)jobs[i].n : 0;
+    return submit(p);
 }
 static int inv_batch_impl(kgbwt_inv_job *jobs, int32_t count, uint32_t flags) {
-    Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
-    return run_inv_jobs(C.w, jobs, count, flags);
+    Pending p{1, jobs, count, flags, 0};
+    for (int32_t i = 0; i < count; i++) p.bytes += jobs[i].n > 0 ? (u64)jobs[i].n : 0;
+    return submit(p);
 }
 
 }  // namespace kgb
@@ -580,6 +703,15 @@ int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg) {
     cfg[0] = c.tile_cap; cfg[1] = c.tile_ctas; cfg[2] = c.msd_ctas; cfg[3] = c.small_group; cfg[4] = c.warp_path;
     cfg[5] = c.lsd_round0; cfg[6] = c.lsd_bytes;
     return 0;
+}
+
+int32_t kgbwt_dropin_stats(int64_t *out, int32_t cap) {
+    if (!out || cap < 0) return -1;
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    const int64_t v[7] = {C.calls[0], C.batches[0], C.largest[0], C.calls[1], C.batches[1], C.largest[1], C.retried};
+    for (int32_t i = 0; i < cap && i < 7; i++) out[i] = v[i];
+    return 7;
 }
 
 const char *kgbwt_last_error(void) { return g_err; }

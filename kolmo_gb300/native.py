@@ -103,6 +103,8 @@ def lib():
     L.kgbwt_engine_profile_read.restype = _I32
     L.kgbwt_kernel_name.argtypes = [_I32]
     L.kgbwt_kernel_name.restype = ctypes.c_char_p
+    L.kgbwt_dropin_stats.argtypes = [_P, _I32]
+    L.kgbwt_dropin_stats.restype = _I32
     L.kgbwt_unbwt_noalloc.argtypes = [_P, _P, _I32, _I32, _P]
     L.kgbwt_unbwt_noalloc.restype = _I32
     L.kgbwt_server_create.argtypes = [_I32, ctypes.c_uint64, ctypes.c_uint64]
@@ -155,7 +157,7 @@ EXPORTS = (
     "kgbwt_engine_create", "kgbwt_engine_destroy", "kgbwt_engine_config", "kgbwt_engine_fwd", "kgbwt_engine_inv",
     "kgbwt_engine_wait", "kgbwt_engine_stats", "kgbwt_engine_workspace_bytes", "kgbwt_last_error", "kgbwt_version",
     "kgbwt_engine_profile", "kgbwt_engine_profile_read", "kgbwt_kernel_name", "kgbwt_engine_option",
-    "kgbwt_unbwt_noalloc", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
+    "kgbwt_unbwt_noalloc", "kgbwt_dropin_stats", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
     "kgbwt_server_cancel", "kgbwt_server_stats_read", "kgbwt_server_inject_oom", "kgbwt_server_plan",
     "kgbwt_estimate_bytes", "kgbwt_engine_last_config", "kgbwt_tuning_load", "kgbwt_tuning_lookup",
     "libcubwt_allocate_device_storage", "libcubwt_free_device_storage", "libcubwt_bwt_aux", "libcubwt_bwt",

@@ -2,6 +2,7 @@
 oracle. Bit-exact: U, the sampled indexes and the suffix array. Cases follow the reference's own tests
 (tests/test_bwt.c:97-121 kinds and sizes; tests/test_gpu_sa.c:74-98 edge kinds and random inputs with repeats)."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -143,10 +144,23 @@ def test_full_size_prose_round_trip_and_oracle():
     assert rc == 0 and np.array_equal(back, T)
 
 
+def _pin_forward(T, r, U, I):
+    """Checks U and every sampled index of a large block: against the reference's own sorter where it was built on
+    this machine (all host threads), else with the oracle's segment decoder, which decodes segment t of the text from
+    I[t + 1] (a wrong sampled index corrupts its segment) and segment 0 from I[0]."""
+    if O.ref_lib() is not None:
+        rc, rU, rI = O.bwt_aux(T, r, use_ref=True, threads=os.cpu_count() or 1)
+        assert rc == 0 and np.array_equal(I, rI), (I, rI)
+        assert np.array_equal(U, rU)
+    else:
+        assert I.size > 1
+        orc, back = O.unbwt_aux(U, r, I, threads=8)
+        assert orc == 0 and np.array_equal(back, T)
+
+
 def test_full_size_degenerate_blocks():
     """The 128 MiB degenerate inputs (periodic with periods 1, 7 and 4096 and one random flip per MiB; Fibonacci
-    word): the GPU inverse restores the text from the GPU forward; for periodic-1 and Fibonacci the oracle's inverse
-    (an LF walk restated from the reference) also decodes the GPU's BWT and sampled indexes."""
+    word): the GPU inverse restores the text from the GPU forward, and U with all its sampled indexes is pinned."""
     n = 128 << 20
     r = 1 << codec18_rlog(n)
     for kind in ("periodic-1", "periodic-7", "periodic-4096", "fibonacci"):
@@ -155,17 +169,14 @@ def test_full_size_degenerate_blocks():
         assert rc == 0, (kind, native.last_error())
         rc, back = codec.unbwt_aux(U, r, I)
         assert rc == 0 and np.array_equal(back, T), kind
-        if kind in ("periodic-1", "fibonacci"):
-            orc, oback = O.unbwt_aux(U, r, I)
-            assert orc == 0 and np.array_equal(oback, T), kind
+        _pin_forward(T, r, U, I)
 
 
 @pytest.mark.parametrize("mib", [24, 64])
 def test_blocks_with_ranked_passes(mib):
     """Blocks of more than 16 M suffixes in a batch of at most 64 M write round 0's ranks in passes over id ranges
-    (24 MiB: two passes, the last one partial; 64 MiB: four): the GPU inverse restores the text, and for 24 MiB the
-    oracle's inverse decodes the GPU's BWT and sampled indexes as well (the BWT is a bijection, so this pins the
-    forward's output)."""
+    (24 MiB: two passes, the last one partial; 64 MiB: four): the GPU inverse restores the text, and U with all its
+    sampled indexes is pinned."""
     n = mib << 20
     T = W.zipf_prose(n, 600 + mib)
     r = 1 << codec18_rlog(n)
@@ -173,6 +184,4 @@ def test_blocks_with_ranked_passes(mib):
     assert rc == 0, native.last_error()
     rc, back = codec.unbwt_aux(U, r, I)
     assert rc == 0 and np.array_equal(back, T)
-    if mib == 24:
-        orc, oback = O.unbwt_aux(U, r, I)
-        assert orc == 0 and np.array_equal(oback, T)
+    _pin_forward(T, r, U, I)

@@ -1,0 +1,160 @@
+"""Whole-frame parity of codec 18 (levels -8 and -9) with the GPU sorter linked into the reference's CLI.
+
+Two binaries are built by ``oracle/Makefile`` (target ``frames``) from the reference's own sources, staged by
+``oracle/stage_ref.py``: ``kolmo-ref``, the reference CLI with its sorter ``src/algo/sais/sais.c``, and ``kolmo-gpu``,
+the same objects with ``libkgbwt.so`` linked in place of ``sais.c`` (the only callers, src/codecs/bwt_stream.c:52,
+73-74, 233 and 294, are unchanged). Pinned three ways:
+
+* the reference's determinism digests: the frames of the reference's seeded generator
+  (benchmark/determinism/check.py) at -8 and -9, with 1 and 4 threads, must have the SHA-256 digests the reference
+  pinned in benchmark/determinism/expected.sha256, and decode back;
+* the reference CLI itself on seeded inputs of the benchmark's sources (the 1 MiB order-2 Markov block, Zipf word
+  prose up to two 32 MiB blocks at -8, the -9 planner's slice trials): byte-identical frames, and each CLI decodes
+  the other's frames;
+* frames written by reference releases (tests/v12/*.kolmo) decode to the originals' digests (tests/v12.sha256).
+
+``KGBWT_STATS`` makes the GPU library log its batches, which shows that the block sorts ran on the GPU."""
+import ast
+import hashlib
+import os
+import random
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+import stage_ref
+from kolmo_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+ORACLE = os.path.dirname(os.path.abspath(stage_ref.__file__))
+TREE = stage_ref.staged() or stage_ref.stage()
+if TREE is None:
+    pytest.skip("the reference's sources are not staged (python oracle/stage_ref.py where the tree is mounted)",
+                allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def clis():
+    r = subprocess.run(["make", "-C", ORACLE, f"REF={TREE}", "-j", str(os.cpu_count() or 4), "frames"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
+    return os.path.join(ORACLE, "_ref", "kolmo-ref"), os.path.join(ORACLE, "_ref", "kolmo-gpu")
+
+
+def _run(cmd, env=None):
+    r = subprocess.run(cmd, capture_output=True, env=env)
+    assert r.returncode == 0, (cmd, r.stderr.decode(errors="replace")[-500:])
+
+
+def _sha(path: str) -> str:
+    return hashlib.sha256(open(path, "rb").read()).hexdigest()
+
+
+class GpuLog:
+    """KGBWT_STATS file of the GPU CLI: one line per batch the library ran."""
+
+    def __init__(self, tmp):
+        self.path = os.path.join(str(tmp), "kgbwt_stats.log")
+        self.env = dict(os.environ, KGBWT_STATS=self.path)
+        self.env.pop("KOLMO_MEMLIMIT", None)
+
+    def lines(self):
+        return open(self.path).read().splitlines() if os.path.exists(self.path) else []
+
+    def calls(self, kind: str) -> int:
+        return sum(int(x.split()[1].split("=")[1]) for x in self.lines() if x.startswith(kind))
+
+
+def _determinism_inputs():
+    """The inputs of the reference's determinism check: its `inputs()` generator, taken from the staged
+    benchmark/determinism/check.py and run here (the module itself runs the check on import)."""
+    path = os.path.join(TREE, "benchmark", "determinism", "check.py")
+    tree = ast.parse(open(path).read(), path)
+    fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == "inputs")
+    ns = {"random": random, "struct": struct}
+    exec(compile(ast.Module(body=[fn], type_ignores=[]), path, "exec"), ns)
+    return [(name, data) for name, data, _ in ns["inputs"]()]
+
+
+def _expected_digests():
+    out = {}
+    for line in open(os.path.join(TREE, "benchmark", "determinism", "expected.sha256")):
+        parts = line.rstrip("\n").split("  ")
+        if len(parts) == 3:
+            out[(parts[1], parts[2])] = parts[0]
+    return out
+
+
+def test_determinism_digests_at_levels_8_and_9(clis, tmp_path):
+    _, gpu = clis
+    log = GpuLog(tmp_path)
+    want = _expected_digests()
+    checked = 0
+    for name, data in _determinism_inputs():
+        p = str(tmp_path / name)
+        open(p, "wb").write(data)
+        for level in ("-8", "-9"):
+            digests = set()
+            for t in ("1", "4"):
+                z, back = p + ".k", p + ".back"
+                _run([gpu, level, "-f", "-T", t, p, "-o", z], log.env)
+                _run([gpu, "-d", "-f", z, "-o", back], log.env)
+                assert open(back, "rb").read() == data, (name, level, t)
+                digests.add(_sha(z))
+            assert digests == {want[(name, level)]}, (name, level, digests)
+            checked += 1
+    assert checked == 22
+    assert log.calls("fwd") > 0 and log.calls("inv") > 0, "no block was sorted by the GPU library"
+
+
+def _frame_inputs():
+    return [("markov1mib", W.markov2(1 << 20, 0xC0FFEE), ("-8", "-9"), ("1",)),
+            ("prose8mib", W.zipf_prose(8 << 20, 811), ("-8", "-9"), ("1", "4")),
+            ("prose48mib", W.zipf_prose(48 << 20, 4811), ("-8",), ("4",)),  # two blocks (32 + 16 MiB) at once
+            ("acgt4mib", W.acgt(4 << 20, 77), ("-9",), ("1",)),
+            ("logs6mib", W.logs(6 << 20, 78), ("-8",), ("2",))]
+
+
+def test_frames_equal_reference_cli(clis, tmp_path):
+    ref, gpu = clis
+    log = GpuLog(tmp_path)
+    for name, T, levels, threads in _frame_inputs():
+        p = str(tmp_path / name)
+        T.tofile(p)
+        for level in levels:
+            for t in threads:
+                zr, zg = p + ".ref.k", p + ".gpu.k"
+                _run([ref, level, "-f", "-T", t, p, "-o", zr])
+                before = log.calls("fwd")
+                _run([gpu, level, "-f", "-T", t, p, "-o", zg], log.env)
+                assert log.calls("fwd") > before, (name, level, "no codec-18 block")
+                assert open(zr, "rb").read() == open(zg, "rb").read(), (name, level, t)
+                for dec, z in ((gpu, zr), (ref, zg), (gpu, zg)):
+                    back = p + ".back"
+                    _run([dec, "-d", "-f", z, "-o", back], log.env)
+                    assert np.array_equal(np.fromfile(back, np.uint8), T), (name, level, t, dec)
+
+
+def test_reference_release_frames_decode(clis, tmp_path):
+    _, gpu = clis
+    log = GpuLog(tmp_path)
+    v12 = os.path.join(TREE, "tests", "v12")
+    digests = {}
+    for line in open(os.path.join(TREE, "tests", "v12.sha256")):
+        parts = line.split()
+        if len(parts) == 2:
+            digests[parts[1]] = parts[0]
+    decoded = 0
+    for line in open(os.path.join(v12, "MANIFEST")):
+        parts = line.split()
+        if len(parts) != 2 or not os.path.exists(os.path.join(v12, parts[0])) or parts[1] not in digests:
+            continue
+        out = str(tmp_path / "out")
+        _run([gpu, "-d", "-f", os.path.join(v12, parts[0]), "-o", out], log.env)
+        assert _sha(out) == digests[parts[1]], parts[0]
+        decoded += 1
+    assert decoded >= 50
+    assert log.calls("inv") > 0, "no frame of the corpus reached the GPU inverse"
