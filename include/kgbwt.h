@@ -150,11 +150,12 @@ const char *kgbwt_kernel_name(int32_t kernel);
  * not grow after start-up): the inverse BWT of one block with all scratch in a static device array inside this
  * library, sized for n <= 262144 bytes (about 2.5 MB, held on every GPU that loads the library until exit).
  * dU: the block's BWT string (sentinel removed, as the drop-in U), dT: the decoded text, both device buffers of n
- * bytes; p0 = I[0]. Returns 0, -1 for bad arguments, n above the maximum, or a string that is not a valid BWT,
- * -2 for a CUDA error. The call waits for its work on `stream` (a cudaStream_t, NULL = the legacy default stream).
- * It calls no device allocator. Every call uses the same static array: calls that overlap on the GPU (from two
- * host threads, or on two streams) race and corrupt each other. The first call on each device looks up the array's
- * device address; make that first call before any stream capture. */
+ * bytes; p0 = I[0]. Returns 0, -1 for bad arguments (a buffer that is not device or managed memory included), n
+ * above the maximum, a string that is not a valid BWT, or a stream that is being captured, -2 for a CUDA error. The
+ * call waits for its work on `stream` (a cudaStream_t, NULL = the legacy default stream) and reads its status back,
+ * so it cannot be called while that stream is capturing. It calls no device allocator. Every call uses the same
+ * static array: calls that overlap on the GPU (from two host threads, or on two streams) race and corrupt each
+ * other. The first call on each device looks up the array's device address (with that device current). */
 int32_t kgbwt_unbwt_noalloc(const uint8_t *dU, uint8_t *dT, int32_t n, int32_t p0, void *stream);
 
 /* ---- request server -----------------------------------------------------------------------------------------------
@@ -203,8 +204,9 @@ uint64_t kgbwt_estimate_bytes(int32_t kind, const int32_t *n, const int32_t *r, 
  * src/core/compress.c:221, src/core/decode.c:405). Every call of sections 1 and 2 queues on the library's default
  * worker; the first caller to find it idle runs the oldest pending call together with every later pending call of
  * the same direction, in arrival order, while their input stays within KGBWT_BATCH_MIB (environment, default 256)
- * MiB, and the other callers wait. If such a combined batch fails at the device level (-2), each of its calls is run
- * again alone. With KGBWT_STATS=<path> in the environment every batch appends one line to that file.
+ * MiB, and the other callers wait. A job's own failure (bad arguments, a string that is no BWT) stays with that job;
+ * if the combined batch fails as a whole (device memory, a layout too large), each of its calls is run again alone.
+ * With KGBWT_STATS=<path> in the environment every batch appends one line to that file.
  * kgbwt_dropin_stats writes up to cap of: forward calls, forward batches, largest forward batch (calls), inverse
  * calls, inverse batches, largest inverse batch, combined batches retried call by call; returns 7. */
 int32_t kgbwt_dropin_stats(int64_t *out, int32_t cap);

@@ -416,25 +416,35 @@ static void run_coalesced(Context &C, std::vector<Pending *> &take) {
         }
         rc = kind ? run_inv_jobs(C.w, ij.data(), (int32_t)ij.size(), flags)
                   : run_fwd_jobs(C.w, fj.data(), (int32_t)fj.size(), flags);
-        if (rc == -2) {
-            // a device-level failure of the combined batch (out of memory, most likely): each call runs alone, so
-            // the result of a call never depends on what it was batched with
+        // Per-job outcomes (bad arguments, a string that is no BWT) are in the jobs' rc and stay with their jobs. A
+        // failure of the combined batch as a whole (device memory, a batch too large to lay out) fails every job:
+        // then each call runs again alone, so that a call's result never depends on what it was batched with.
+        bool whole = rc == -2;
+        if (rc && !whole) {
+            whole = true;
+            for (size_t i = 0; i < total && whole; i++) whole = (kind ? ij[i].rc : fj[i].rc) != 0;
+        }
+        if (whole) {
             std::lock_guard<std::mutex> lock(C.mu);
             C.retried++;
         }
         size_t k = 0;
         for (Pending *p : take) {
-            if (rc == -2) {
+            bool failed = false;
+            if (whole) {
                 p->rc = kind ? run_inv_jobs(C.w, (kgbwt_inv_job *)p->jobs, p->count, flags)
                              : run_fwd_jobs(C.w, (kgbwt_fwd_job *)p->jobs, p->count, flags);
+                failed = p->rc != 0;
             } else {
                 for (int32_t i = 0; i < p->count; i++, k++) {
-                    if (kind) ((kgbwt_inv_job *)p->jobs)[i].rc = ij[k].rc;
-                    else ((kgbwt_fwd_job *)p->jobs)[i].rc = fj[k].rc;
+                    const int32_t jr = kind ? ij[k].rc : fj[k].rc;
+                    if (kind) ((kgbwt_inv_job *)p->jobs)[i].rc = jr;
+                    else ((kgbwt_fwd_job *)p->jobs)[i].rc = jr;
+                    failed = failed || jr != 0;
                 }
-                p->rc = rc;
+                p->rc = 0;
             }
-            if (p->rc) snprintf(p->err, sizeof p->err, "%s", g_err);
+            if (failed) snprintf(p->err, sizeof p->err, "%s", g_err);
         }
     }
     log_batch(kind, take.size(), total, bytes, rc);
@@ -469,7 +479,7 @@ static int submit(Pending &p) {
         C.busy = false;
         C.cv.notify_all();
     }
-    if (p.rc || p.err[0]) record_error(p.err);
+    if (p.err[0]) record_error(p.err);
     return p.rc;
 }
 

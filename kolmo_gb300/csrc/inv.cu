@@ -691,5 +691,23 @@ extern "C" int32_t kgbwt_unbwt_noalloc(const uint8_t *dU, uint8_t *dT, int32_t n
         kgb::record_error("kgbwt_unbwt_noalloc: n exceeds the maximum of 262144 bytes of the static scratch");
         return -1;
     }
+    // both buffers must be memory the device can address (device or managed allocations): a host pointer would
+    // send the kernels to an address they cannot use
+    for (const void *p : {(const void *)dU, (const void *)dT}) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess ||
+            (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+            cudaGetLastError();
+            kgb::record_error("kgbwt_unbwt_noalloc: dU and dT must be device (or managed) memory");
+            return -1;
+        }
+    }
+    // every call reads its status back and waits for the stream, which a stream under capture does not allow
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        kgb::record_error("kgbwt_unbwt_noalloc: the stream is being captured; this call synchronises with it");
+        return -1;
+    }
     return kgb::unbwt_noalloc(dU, dT, (kgb::u32)n, (kgb::u32)p0, (cudaStream_t)stream);
 }

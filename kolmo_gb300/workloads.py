@@ -1,7 +1,6 @@
 """Seeded synthetic inputs for the BWT path (bindings to ``csrc/workloads.c``).
 
-Sources: the reference's BWT test blocks (tests/test_bwt.c:24-45 kinds 0-8), order-2 Markov bytes over 64 symbols
-with Dirichlet(0.3) rows, Zipf(1.1) word prose with verbatim repeats, ACGT with 0.1% N, templated log lines, periodic
+Sources: order-2 Markov bytes over 64 symbols with Dirichlet(0.3) rows, Zipf(1.1) word prose with verbatim repeats, ACGT with 0.1% N, templated log lines, periodic
 text with one flip per MiB and the Fibonacci word; plus the size distributions of the mixed batch (log-uniform
 16 KiB-16 MiB) and of the request stream (lognormal, median 256 KiB, sigma 1.5, capped at 128 MiB). The same seed
 gives the same bytes on every machine.
@@ -27,7 +26,6 @@ def lib():
         if not os.path.exists(path):
             _build.build_workloads()
         L = ctypes.CDLL(path)
-        L.kgw_test_block.argtypes = [ctypes.c_int, ctypes.c_int, _P]
         L.kgw_markov2.argtypes = [_P, _U64, _U64, ctypes.c_int, ctypes.c_double]
         L.kgw_zipf_prose.argtypes = [_P, _U64, _U64, ctypes.c_int, ctypes.c_double, ctypes.c_uint32, ctypes.c_int,
                                      ctypes.c_uint32, ctypes.c_uint32]
@@ -57,13 +55,6 @@ def _buf(n: int, out: np.ndarray | None):
 def _check(rc: int, what: str):
     if rc != 0:
         raise RuntimeError(f"{what} failed ({rc})")
-
-
-def test_block(kind: int, n: int) -> np.ndarray:
-    """The reference's suffix-sorter test block of the given kind (0-8) and size."""
-    out = np.empty(max(n, 1), np.uint8)
-    lib().kgw_test_block(kind, n, out.ctypes.data)
-    return out[:n]
 
 
 def markov2(n: int, seed: int, nsym: int = 64, alpha: float = 0.3, out=None) -> np.ndarray:

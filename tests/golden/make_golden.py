@@ -4,7 +4,7 @@ Run in a checkout where the reference tree is mounted and ``make -C oracle`` has
 from the reference's src/algo/sais/sais.c and src/algo/par.c. For every case the script records hashes of the
 reference's BWT (U), its sampled indexes (I) and the suffix array implied by them (derived by the LF walk, since the
 reference exposes no suffix array), plus a hash of the input so that a machine regenerating the input can check it
-got the same bytes. Inputs come from kolmo_gb300.workloads (deterministic on every platform).
+got the same bytes. Inputs come from kolmo_gb300.workloads and tests/refgen.py (deterministic on every platform).
 
 Cases:
   * the reference's own suffix-sorter test matrix (tests/test_bwt.c:97-121): block kinds 0-8 of its generator, the
@@ -25,9 +25,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import oracle as O  # noqa: E402
-from kolmo_gb300 import workloads as W  # noqa: E402
+from kolmo_gb300 import workloads as W
+import refgen as R  # noqa: E402
 from kolmo_gb300.host import codec18_rlog  # noqa: E402
 
 TEST_SIZES = [2, 3, 7, 100, 4096, 65536, 70001, 300000, 1000003]
@@ -58,7 +60,7 @@ def main() -> None:
     cases = []
     for kind in range(9):
         for n in TEST_SIZES:
-            T = W.test_block(kind, n)
+            T = R.test_block(kind, n)
             for rl in (1, 10, 19):
                 r = 1 << rl
                 if (n - 1) // r > 1000:
@@ -81,7 +83,7 @@ def main() -> None:
     T = W.zipf_prose(4 << 20, 77, ncopies=20)
     cases.append(dict(case("prose/4194304", T, 1 << codec18_rlog(T.size)), gen="prose", seed=77, ncopies=20))
     for i, (kind, n, r) in enumerate(((8, 40, 2), (3, 17, 4), (1, 64, 8), (0, 9, 2), (7, 100, 16))):
-        T = W.test_block(kind, n)
+        T = R.test_block(kind, n)
         cases.append(dict(case(f"tiny/{i}", T, r, full=True), gen="test_block", kind=kind))
     out = {"generator": "tests/golden/make_golden.py", "sorter": "reference src/algo/sais/sais.c (libsais 2.12.1 subset)",
            "hash": "fnv-1a 64", "cases": cases}

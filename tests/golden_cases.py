@@ -6,6 +6,7 @@ import os
 import numpy as np
 
 from kolmo_gb300 import workloads as W
+import refgen as R
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -18,7 +19,7 @@ def load():
 def make_input(c) -> np.ndarray:
     g = c["gen"]
     if g == "test_block":
-        return W.test_block(c["kind"], c["n"])
+        return R.test_block(c["kind"], c["n"])
     if g == "markov_1mib":
         return W.markov_1mib()
     if g == "source":

@@ -5,6 +5,7 @@ import pytest
 import oracle as O
 from kolmo_gb300 import codec
 from kolmo_gb300 import workloads as W
+import refgen as R
 
 pytestmark = pytest.mark.gpu
 
@@ -96,7 +97,7 @@ def test_round0_paths_on_mixed_batch(lsd_round0, lsd_bytes):
     import torch
 
     texts = [np.array([7, 1], np.uint8), np.array([3, 3], np.uint8), np.full(20_000, 97, np.uint8),
-             W.periodic(60_000, 11, 7, 1 << 14), W.markov2(90_000, 12), W.test_block(5, 5_000),
+             W.periodic(60_000, 11, 7, 1 << 14), W.markov2(90_000, 12), R.test_block(5, 5_000),
              np.array([5, 0, 5, 0, 5, 0, 5, 0, 5, 0, 5], np.uint8), np.zeros(3_000, np.uint8),
              W.zipf_prose(150_000, 13), np.array([2, 1, 2], np.uint8)]
     buf, offs = _pack(texts)

@@ -11,6 +11,7 @@ import oracle as O
 from golden_cases import h, make_input
 from kolmo_gb300 import codec, native
 from kolmo_gb300 import workloads as W
+import refgen as R
 from kolmo_gb300.host import codec18_rlog
 
 pytestmark = pytest.mark.gpu
@@ -120,7 +121,7 @@ def test_suffix_array_output_matches_oracle():
     import torch
 
     eng = codec.Engine()
-    for T in (W.markov2(300_000, 5), W.periodic(200_000, 3, 7, 1 << 16), W.test_block(8, 250_000)):
+    for T in (W.markov2(300_000, 5), W.periodic(200_000, 3, 7, 1 << 16), R.test_block(8, 250_000)):
         n = T.size
         dT = torch.zeros(n + 64, dtype=torch.uint8, device="cuda")
         dT[:n] = torch.from_numpy(T).cuda()

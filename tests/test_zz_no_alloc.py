@@ -49,3 +49,29 @@ def test_no_alloc_refuses_oversize_and_bad_arguments():
     assert lib.kgbwt_unbwt_noalloc(p, p, 100, 0, None) == -1
     assert lib.kgbwt_unbwt_noalloc(p, p, 100, 101, None) == -1
     assert lib.kgbwt_unbwt_noalloc(None, p, 100, 1, None) == -1
+    host = np.zeros(1000, np.uint8)  # a host buffer is refused before any kernel sees it
+    assert lib.kgbwt_unbwt_noalloc(host.ctypes.data, p, 1000, 1, None) == -1
+    assert lib.kgbwt_unbwt_noalloc(p, host.ctypes.data, 1000, 1, None) == -1
+
+
+def test_no_alloc_reports_an_invalid_string_and_stays_usable():
+    """A string that is no BWT for its primary index returns -1 from the status word; the next valid call on the same
+    static scratch still decodes like the existing entry point."""
+    import torch
+
+    lib = native.lib()
+    n = 1000
+    # 'a' * n with the sentinel in row 1: rows 0 and 1 form an LF cycle of their own
+    dU = torch.full((n,), ord("a"), dtype=torch.uint8, device="cuda")
+    dT = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    assert lib.kgbwt_unbwt_noalloc(dU.data_ptr(), dT.data_ptr(), n, 1, None) == -1
+    assert "not a valid BWT" in native.last_error()
+    T, U, I = _case(120_000, 44, 1 << 12)
+    rc_ref, out_ref = codec.unbwt_aux(U, 1 << 12, I)
+    assert rc_ref == 0
+    dU = torch.from_numpy(U.copy()).cuda()
+    dT = torch.zeros(U.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    assert lib.kgbwt_unbwt_noalloc(dU.data_ptr(), dT.data_ptr(), U.size, int(I[0]), None) == 0
+    assert np.array_equal(dT.cpu().numpy(), out_ref)
