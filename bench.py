@@ -314,7 +314,7 @@ def run_ours(args, world, rank, local):
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
     eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0,
-               args.lsd_bytes)
+               args.lsd_bytes, args.chain_from)
     dT = torch.zeros(nmax + 64, dtype=torch.uint8, device=dev)
     dL = torch.zeros(nmax + 1, dtype=torch.uint8, device=dev)
     dI = torch.zeros(n_samples(nmax, 2), dtype=torch.int32, device=dev)
@@ -536,7 +536,7 @@ def run_batch(args, world, rank, local):
     s = torch.cuda.Stream(device=dev)
     eng = codec.Engine()
     eng.config(args.tile_cap, args.tile_ctas, args.msd_ctas, args.small_group, args.warp_path, args.lsd_round0,
-               args.lsd_bytes)
+               args.lsd_bytes, args.chain_from)
     fblocks = [(off, int(t.size), r, io) for t, off, r, io in zip(texts, offs, rs, iouts)]
 
     def to_u(b_list, I):
@@ -874,6 +874,7 @@ def main():
     ap.add_argument("--warp-path", type=int, default=-1)
     ap.add_argument("--lsd-round0", type=int, default=-1)
     ap.add_argument("--lsd-bytes", type=int, default=-1, help="prefix bytes of the LSD round 0 (8, 12 or 16)")
+    ap.add_argument("--chain-from", type=int, default=-1, help="first rank round with repeat chains (0: none)")
     ap.add_argument("--profile-out", default="", help="write the per-launch profile of the profiled step here")
     ap.add_argument("--plain", action="store_true",
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")

@@ -93,11 +93,15 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
  * KGBWT_OPT_LSD_ROUND0 (0/1, default 1): the first round (all suffixes by their prefix) is one LSD radix sort of the
  *   whole batch; 0: bucket passes and tile kernels over 8-byte prefixes as in the later rounds.
  * KGBWT_OPT_LSD_BYTES (8, 12 or 16, default 16): prefix bytes that LSD round sorts (16 replaces the first rank round;
- *   the rank rounds then double from there). */
+ *   the rank rounds then double from there).
+ * KGBWT_OPT_CHAIN_FROM (0..64, default 1): from this rank round on, a group of two suffixes that doubling leaves
+ *   together is also ordered along its repeat chain (the pairs of the two copies of a repeat, ordered where the
+ *   repeat ends) instead of waiting for the doubling to reach the repeat's end; 0: never. */
 #define KGBWT_OPT_SMALL_GROUP 1
 #define KGBWT_OPT_WARP_PATH 2
 #define KGBWT_OPT_LSD_ROUND0 3
 #define KGBWT_OPT_LSD_BYTES 4
+#define KGBWT_OPT_CHAIN_FROM 5
 int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value);
 /* The configuration the engine's last forward call ran with: tile_cap, tile_ctas, msd_ctas, small_group, warp_path,
  * lsd_round0, lsd_bytes (cfg[0..6]). Fields the caller set with kgbwt_engine_config / kgbwt_engine_option are used as set; the

@@ -112,11 +112,12 @@ class Engine:
             self.config(tile_cap, tile_ctas, msd_ctas)
 
     def config(self, tile_cap: int = 0, tile_ctas: int = 0, msd_ctas: int = 0, small_group: int = -1,
-               warp_path: int = -1, lsd_round0: int = -1, lsd_bytes: int = -1):
+               warp_path: int = -1, lsd_round0: int = -1, lsd_bytes: int = -1, chain_from: int = -1):
         L = native.lib()
         rc = L.kgbwt_engine_config(self.h, tile_cap, tile_ctas, msd_ctas)
         for opt, val in ((native.OPT_SMALL_GROUP, small_group), (native.OPT_WARP_PATH, warp_path),
-                         (native.OPT_LSD_ROUND0, lsd_round0), (native.OPT_LSD_BYTES, lsd_bytes)):
+                         (native.OPT_LSD_ROUND0, lsd_round0), (native.OPT_LSD_BYTES, lsd_bytes),
+                         (native.OPT_CHAIN_FROM, chain_from)):
             if rc == 0 and val >= 0:
                 rc = L.kgbwt_engine_option(self.h, opt, val)
         if rc:

@@ -27,7 +27,7 @@ const char *kernel_name(int k) {
         "tile_warp_prefix", "tile_warp_prefix_keyed", "tile_warp_rank", "tile_warp_rank_keyed",
         "lsd_begin", "lsd_key0", "lsd_hist", "lsd_pass", "seg_count", "seg_scan", "seg_emit1", "seg_emit2",
         "group_thread", "group_warp", "mkeys", "lsd_ident", "seg_rank",
-        "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit"};
+        "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit", "chain"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
 
@@ -335,6 +335,7 @@ static int parse_tuning(const char *text, std::vector<TuneBucket> &out) {
             else if (key == "warp_path") { if (v != 0 && v != 1) return -1; b.c.warp_path = (int)v; }
             else if (key == "lsd_round0") { if (v != 0 && v != 1) return -1; b.c.lsd_round0 = (int)v; }
             else if (key == "lsd_bytes") { if (v != 8 && v != 12 && v != 16) return -1; b.c.lsd_bytes = (int)v; }
+            else if (key == "chain_from") { if (v < 0 || v > 64) return -1; b.c.chain_from = (int)v; }
         }
         if (!have_max) return -1;
         out.push_back(b);
@@ -584,6 +585,11 @@ int32_t kgbwt_engine_option(kgbwt_engine *e, int32_t option, int32_t value) {
             if (value != 8 && value != 12 && value != 16) return -1;
             e->fwd.ucfg.lsd_bytes = value;
             e->fwd.cfg_explicit |= CFG_LSD_BYTES;
+            return 0;
+        case KGBWT_OPT_CHAIN_FROM:
+            if (value < 0 || value > 64) return -1;
+            e->fwd.ucfg.chain_from = value;
+            e->fwd.cfg_explicit |= CFG_CHAIN_FROM;
             return 0;
         default:
             return -1;

@@ -74,6 +74,10 @@ struct FwdArgs {
     u32 *lhist, *ltile, *segagg;
     u32 *lbase;  // round 0: per block and digit slot, the pass's first position of every digit
     u32 spin_limit;
+    // chains of repeat pairs (rank rounds >= chain_from): bit x of cbits = the pair of suffix x continues at x + 1;
+    // cnz / ctn: the next-zero tables over cbits' words (see k_chain_nz)
+    u32 *cbits, *cnz, *ctn;
+    u32 cwords, ctiles, chain_from;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segk, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
 };
@@ -813,6 +817,135 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------------------------------ repeat chains
+// Two suffixes a and b in one group have equal first characters, so they sort as a + 1 and b + 1 do. In a repeat
+// (two equal stretches of text) the pairs {a, b}, {a + 1, b + 1}, ... are groups of two round after round until the
+// doubling step reaches the end of the repeat, about log2(length / h) rounds later. The chain kernels order such
+// pairs in one step: for every pair {a, b} of this round's tiny list, bit a and bit b of cbits say that a + 1 and
+// b + 1 are in one group now (so a's chain continues at a + 1, whose group, if it is a pair, is {a + 1, b + 1}). The
+// first clear bit e >= a ends a's chain, and the pair sorts as the suffixes e + 1 and b + (e - a) + 1 do: by their
+// current ranks when those differ, the shorter first when one of them lies past the block end, else not yet.
+// (Each id has one partner, so chains of different pairs never overlap inconsistently: the chain from a would have
+// to pass through b's own group to meet b's chain, and b's group is {a, b}.)
+constexpr u32 NZ_TILE = 4096;  // words per tile of the next-zero table
+constexpr u32 NZ_NONE = 0xFFFFFFFFu;
+
+__device__ __forceinline__ bool chain_on(const FwdArgs &a) {
+    const Ctl *c = a.ctl;
+    return a.chain_from && c->round >= a.chain_from && (u32)c->cnt[L_P0 + c->rpar] != 0;
+}
+
+__global__ void __launch_bounds__(TPB) k_chain_clear(FwdArgs a) {
+    if (!chain_on(a)) return;
+    for (u32 w = blockIdx.x * TPB + threadIdx.x; w < a.cwords; w += gridDim.x * TPB) a.cbits[w] = 0;
+}
+
+// Bits of the pairs whose successors share a group.
+__global__ void __launch_bounds__(TPB) k_chain_link(FwdArgs a) {
+    if (!chain_on(a)) return;
+    const Ctl *ctl = a.ctl;
+    const u32 rpar = ctl->rpar;
+    const ListView in = a.lists[L_P0 + rpar];
+    const u32 nseg = min((u32)(ctl->cnt[L_P0 + rpar] >> 32), (u32)a.cap_segt), nslots = min(ctl->p_alloc, (u32)a.cap_n);
+    const u32 *isa = a.isa[rpar];
+    for (u32 s = blockIdx.x * TPB + threadIdx.x; s < nseg; s += gridDim.x * TPB) {
+        const Seg g = in.seg[s];
+        if (g.len != 2 || (u64)g.start + 2 > nslots) continue;
+        const u32 x = in.eid[g.start], y = in.eid[g.start + 1];
+        const u64 end = blk_end(a, seg_blk(g.bd));
+        if ((u64)x + 1 >= end || (u64)y + 1 >= end) continue;
+        if (__ldg(isa + x + 1) != __ldg(isa + y + 1)) continue;
+        if (KGB_OK((x >> 5) < a.cwords && (y >> 5) < a.cwords, &a.ctl->err, E_RANK)) {
+            atomicOr(a.cbits + (x >> 5), 1u << (x & 31));
+            atomicOr(a.cbits + (y >> 5), 1u << (y & 31));
+        }
+    }
+}
+
+// Next-zero table, part 1: for every word w, the first word at or after w within w's tile of NZ_TILE words that has a
+// clear bit (NZ_NONE if none), and per tile the first such word (ctn, NZ_NONE if none). One CTA per tile.
+__global__ void __launch_bounds__(TPB) k_chain_nz(FwdArgs a) {
+    if (!chain_on(a)) return;
+    __shared__ u32 sm[TPB];
+    constexpr u32 PER = NZ_TILE / TPB;
+    for (u32 t = blockIdx.x; t < a.ctiles; t += gridDim.x) {
+        const u32 w0 = t * NZ_TILE + threadIdx.x * PER;
+        u32 loc[PER];
+        u32 nxt = NZ_NONE;  // first word with a clear bit at or after the current one, within this thread's run
+#pragma unroll
+        for (int q = PER - 1; q >= 0; q--) {
+            const u32 w = w0 + q;
+            if (w < a.cwords && a.cbits[w] != 0xFFFFFFFFu) nxt = w;
+            loc[q] = nxt;
+        }
+        sm[threadIdx.x] = nxt;  // this thread's first such word
+        __syncthreads();
+        // the first such word after this thread's run: the minimum over the later threads' runs
+        u32 after = NZ_NONE;
+        for (u32 j = threadIdx.x + 1; j < TPB; j++) {
+            if (sm[j] != NZ_NONE) { after = sm[j]; break; }
+        }
+#pragma unroll
+        for (int q = 0; q < (int)PER; q++) {
+            const u32 w = w0 + q;
+            if (w < a.cwords) a.cnz[w] = loc[q] != NZ_NONE ? loc[q] : after;
+        }
+        if (threadIdx.x == 0) a.ctn[t] = nxt != NZ_NONE ? nxt : after;
+        __syncthreads();
+    }
+}
+
+// Next-zero table, part 2 (one CTA): ctn[t] = the first word with a clear bit in tiles t, t + 1, ... (a suffix
+// minimum over the tiles); ctn[ctiles] is the last word, which is never set.
+__global__ void __launch_bounds__(1024) k_chain_tiles(FwdArgs a) {
+    if (!chain_on(a)) return;
+    __shared__ u32 sm[1024];
+    const u32 nt = a.ctiles;
+    const u32 per = (nt + 1023) / 1024;
+    const u32 t0 = threadIdx.x * per;
+    u32 nxt = NZ_NONE;
+    for (int q = (int)per - 1; q >= 0; q--) {
+        const u32 t = t0 + q;
+        if (t < nt && a.ctn[t] != NZ_NONE) nxt = a.ctn[t];
+    }
+    sm[threadIdx.x] = nxt;
+    __syncthreads();
+    u32 after = a.cwords - 1;
+    for (u32 j = threadIdx.x + 1; j < 1024; j++) {
+        if (sm[j] != NZ_NONE) { after = sm[j]; break; }
+    }
+    for (int q = (int)per - 1; q >= 0; q--) {
+        const u32 t = t0 + q;
+        if (t < nt) {
+            if (a.ctn[t] != NZ_NONE) after = a.ctn[t];
+            a.ctn[t] = after;
+        }
+    }
+    if (threadIdx.x == 0) a.ctn[nt] = a.cwords - 1;
+}
+
+// The end of x's chain: the first id e >= x whose bit is clear.
+__device__ __forceinline__ u32 chain_end(const FwdArgs &a, u32 x) {
+    const u32 w = x >> 5;
+    const u32 z = ~a.cbits[w] & (~0u << (x & 31));
+    if (z) return (w << 5) + __ffs(z) - 1;
+    u32 w2 = w + 1 < a.cwords ? a.cnz[w + 1] : a.cwords - 1;
+    if (w2 == NZ_NONE) w2 = a.ctn[(w + 1) / NZ_TILE + 1];
+    if (!KGB_OK(w2 < a.cwords, &a.ctl->err, E_RANK)) return x;
+    return (w2 << 5) + __ffs(~a.cbits[w2]) - 1;
+}
+
+// The order of the pair {x, y} (one group, this round's ranks isa) from x's chain: -1 when x sorts first, 1 when y
+// does, 0 when the chain ends in a larger group (not decided yet).
+__device__ __forceinline__ int chain_order(const FwdArgs &a, const u32 *__restrict__ isa, u32 x, u32 y, u64 end) {
+    const u32 e = chain_end(a, x);
+    const u64 f = (u64)e + 1, g = (u64)y + (e - x) + 1;
+    if (f >= end) return -1;  // x's side reaches the block end first: the shorter suffix sorts first
+    if (g >= end) return 1;
+    const u32 rf = __ldg(isa + f), rg = __ldg(isa + g);
+    return rf == rg ? 0 : (rf < rg ? -1 : 1);
+}
+
 // ------------------------------------------------------------------------------------------------ tiny groups
 // Rank rounds: one thread per group of at most GTINY suffixes. The thread gathers the group's keys into registers,
 // sorts them with a sorting network (2, 4 or 8 inputs, the widest group of the warp decides), and emits ranks,
@@ -860,6 +993,11 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? ids[g.start + q] : 0u;
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++) k[q] = q < len ? rank_key(isa_cur, v[q], h, end) : 0xFFFFFFFFu;
+        if (len == 2 && k[0] == k[1] && chain_on(a)) {
+            // a pair that doubling leaves together: its repeat chain may order it now
+            const int o = chain_order(a, isa_cur, v[0], v[1], end);
+            if (o) { k[0] = o < 0 ? 0u : 1u; k[1] = o < 0 ? 1u : 0u; }
+        }
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
         if (mlen <= 2) {
             KGB_CS(0, 1);
@@ -1655,6 +1793,11 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_lbase, (size_t)bcap * NSLOT * 256 * 4);
     add((void **)&d_ltile, NSLOT * 4);
     add((void **)&d_segagg, stiles * 8 * 4);
+    // repeat chains: a bit per id, its next-zero table per word and per tile of words
+    const u64 cwords = n / 32 + 2, ctiles = cwords / NZ_TILE + 1;
+    add((void **)&d_cbits, cwords * 4);
+    add((void **)&d_cnz, cwords * 4);
+    add((void **)&d_ctn, (ctiles + 1) * 4);
     add((void **)&d_ctl, sizeof(Ctl));
 }
 
@@ -1733,6 +1876,10 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     a.lkey[0] = lists[L_L0].eid; a.lkey[1] = lists[L_KS].eid;
     a.segbits = d_segbits;
     a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg; a.lbase = d_lbase;
+    a.cbits = d_cbits; a.cnz = d_cnz; a.ctn = d_ctn;
+    a.cwords = (u32)(N / 32 + 2);
+    a.ctiles = (a.cwords + NZ_TILE - 1) / NZ_TILE;
+    a.chain_from = (u32)cfg.chain_from;
     a.spin_limit = 1u << 22;
     a.small_group = (u32)cfg.small_group;
     a.lsd_bytes = (u32)cfg.lsd_bytes;
@@ -1806,6 +1953,7 @@ void FwdEngine::resolve_config() {
     if (!(cfg_explicit & CFG_WARP_PATH)) cfg.warp_path = t.warp_path;
     if (!(cfg_explicit & CFG_LSD_ROUND0)) cfg.lsd_round0 = t.lsd_round0;
     if (!(cfg_explicit & CFG_LSD_BYTES)) cfg.lsd_bytes = t.lsd_bytes;
+    if (!(cfg_explicit & CFG_CHAIN_FROM)) cfg.chain_from = t.chain_from;
 }
 
 static int ceil_log2(u64 x) { int k = 0; while ((1ull << k) < x) k++; return k; }
@@ -2067,6 +2215,20 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
 
 static u32 host_active_slots(const Ctl &c) { return c.lsd_act; }
 
+// The repeat-chain tables of a rank round (each kernel returns at once before round chain_from or on an empty tiny
+// list): clear the bits, set them for the linked pairs, build the next-zero tables.
+static cudaError_t enq_chain(Launcher &L, const FwdArgs &a, u32 elems, u32 segs) {
+    cudaError_t e;
+    L.tag(K_CHAIN, elems, segs);
+    if ((e = L.go(k_chain_clear, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_CHAIN, elems, segs);
+    if ((e = L.go(k_chain_link, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_CHAIN, elems, segs);
+    if ((e = L.go(k_chain_nz, L.grid_msd, TPB, 0, a))) return e;
+    L.tag(K_CHAIN, elems, segs);
+    return L.go(k_chain_tiles, 1, 1024, 0, a);
+}
+
 int FwdEngine::run_plain(cudaStream_t s) {
     const u32 smax = (u32)cfg.tile_cap / 2;
     FwdArgs a = make_args(d_ctl, d_T, d_blk, d_isa, d_L, d_SA, d_I, lists, d_hist, d_cursor, d_bhead, d_orand, d_dest,
@@ -2151,6 +2313,7 @@ int FwdEngine::run_plain(cudaStream_t s) {
                 KGB_CHECK(L.go(k_group_warp, grid_scan, TPB, 0, a));
             }
             if (!prefix && cnt_e(L_P0 + rp)) {
+                if (a.chain_from && (u32)round >= a.chain_from) KGB_CHECK(enq_chain(L, a, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp)));
                 L.tag(K_GROUP, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
                 KGB_CHECK(L.go(k_group_thread, grid_msd, TPB, 0, a));
             }
@@ -2236,6 +2399,7 @@ static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L
         if (prefix) return cudaSuccess;
         if ((e = L.go(k_mkeys, L.grid_msd, TPB, 0, a))) return e;
         if ((e = L.go(k_group_warp, L.grid_scan, TPB, 0, a))) return e;
+        if (a.chain_from && (e = enq_chain(L, a, 0, 0))) return e;
         return L.go(k_group_thread, L.grid_msd, TPB, 0, a);
     });
 }

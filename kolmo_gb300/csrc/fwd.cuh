@@ -72,10 +72,12 @@ struct FwdConfig {
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
     int lsd_round0 = 1;   // round 0 as one LSD radix sort of all suffixes; 0: bucket passes + tiles over 8-byte prefixes
     int lsd_bytes = 16;   // prefix bytes the LSD round 0 sorts (8, 12 or 16)
+    int chain_from = 1;   // first rank round whose pairs are also ordered along their repeat chains (0: never)
 };
 // Fields of FwdConfig a caller set explicitly (they override the tuning table).
 enum : u32 {
-    CFG_TILE_CTAS = 1, CFG_MSD_CTAS = 2, CFG_SMALL_GROUP = 4, CFG_WARP_PATH = 8, CFG_LSD_ROUND0 = 16, CFG_LSD_BYTES = 32
+    CFG_TILE_CTAS = 1, CFG_MSD_CTAS = 2, CFG_SMALL_GROUP = 4, CFG_WARP_PATH = 8, CFG_LSD_ROUND0 = 16, CFG_LSD_BYTES = 32,
+    CFG_CHAIN_FROM = 64
 };
 // The tuning table's configuration for a batch of n text bytes: fills the fields the table sets (tile_ctas,
 // msd_ctas, small_group, warp_path, lsd_round0) and returns true, or returns false when no table is loaded.
@@ -166,6 +168,7 @@ class FwdEngine {
     u64 *d_lstat = nullptr;
     u32 *d_lbase = nullptr;
     u32 *d_lhist = nullptr, *d_ltile = nullptr, *d_segagg = nullptr, *d_segbits = nullptr;
+    u32 *d_cbits = nullptr, *d_cnz = nullptr, *d_ctn = nullptr;  // repeat chains
     u64 lsd_tiles_cap = 0, seg_tiles_cap = 0;
     u8 *d_dest = nullptr;
     Ctl *d_ctl = nullptr;
@@ -190,7 +193,7 @@ class FwdEngine {
                    cfg.tile_cap == o.cfg.tile_cap && cfg.tile_ctas == o.cfg.tile_ctas &&
                    cfg.msd_ctas == o.cfg.msd_ctas && cfg.small_group == o.cfg.small_group &&
                    cfg.warp_path == o.cfg.warp_path && cfg.lsd_round0 == o.cfg.lsd_round0 &&
-                   cfg.lsd_bytes == o.cfg.lsd_bytes && lsd == o.lsd;
+                   cfg.lsd_bytes == o.cfg.lsd_bytes && cfg.chain_from == o.cfg.chain_from && lsd == o.lsd;
         }
     };
     GraphKey graph_key{};

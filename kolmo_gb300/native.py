@@ -42,6 +42,7 @@ OPT_SMALL_GROUP = 1
 OPT_WARP_PATH = 2
 OPT_LSD_ROUND0 = 3
 OPT_LSD_BYTES = 4
+OPT_CHAIN_FROM = 5
 REQ_FWD = 1
 REQ_INV = 2
 

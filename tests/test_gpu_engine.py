@@ -127,6 +127,56 @@ def test_round0_paths_on_mixed_batch(lsd_round0, lsd_bytes):
             assert np.array_equal(np.concatenate([col[:p0], col[p0 + 1:]]), oU), b
 
 
+def _repeats(n, seed):
+    """A random block with long verbatim repeats: stretches of 1-40 KiB copied from earlier positions, some copies of
+    copies, some overlapping their source (periodic runs)."""
+    rng = np.random.default_rng(seed)
+    t = rng.integers(0, 4 if seed % 2 else 256, n).astype(np.uint8)
+    for _ in range(40):
+        L = int(rng.integers(1 << 10, 40 << 10))
+        d = int(rng.integers(1, n - L))
+        s = int(rng.integers(max(0, d - 3 * L), d))
+        for q in range(0, L, max(1, d - s)):  # overlapping copies are made in steps of the distance
+            m = min(d - s, L - q)
+            t[d + q:d + q + m] = t[s + q:s + q + m]
+    return t
+
+
+@pytest.mark.parametrize("chain_from", [0, 1, 3])
+def test_repeat_chains_give_the_doubling_order(chain_from):
+    """Pairs ordered along their repeat chains (from rank round 1, from round 3, or never) give the oracle's BWT and
+    sampled indexes on blocks made of long verbatim repeats, on the plain path and in the captured graph."""
+    import torch
+
+    texts = [_repeats(3 << 20, 1), _repeats(2 << 20, 2), W.zipf_prose(4 << 20, 71),
+             np.concatenate([W.markov2(1 << 20, 5)] * 2), W.periodic(1 << 20, 9, 4096, 1 << 16)]
+    buf, offs = _pack(texts)
+    r = 1 << 14
+    iouts, k = [], 0
+    for t in texts:
+        iouts.append(k)
+        k += (t.size - 1) // r + 1
+    want = [O.bwt_aux(t, r)[1:] for t in texts]
+    dT = torch.from_numpy(buf).cuda()
+    dL = torch.zeros(buf.size + len(texts), dtype=torch.uint8, device="cuda")
+    dI = torch.zeros(k, dtype=torch.int32, device="cuda")
+    eng = codec.Engine()
+    eng.config(chain_from=chain_from)
+    blocks = [(off, t.size, r, io) for t, off, io in zip(texts, offs, iouts)]
+    for it in range(3):  # plain launches, then capture, then the cached graph
+        dL.zero_()
+        assert eng.fwd(dT, dL, dI, blocks) == 0
+        assert eng.wait()[0] == 0
+        L = dL.cpu().numpy()
+        I = dI.cpu().numpy()
+        for b, (t, off, io) in enumerate(zip(texts, offs, iouts)):
+            oU, oI = want[b]
+            assert np.array_equal(I[io:io + oI.size], oI), (chain_from, it, b)
+            col = L[off + b: off + b + t.size + 1]
+            p0 = int(oI[0])
+            assert np.array_equal(np.concatenate([col[:p0], col[p0 + 1:]]), oU), (chain_from, it, b)
+
+
 def test_tuning_table_applies_and_explicit_settings_win(tmp_path):
     import json
     import os
