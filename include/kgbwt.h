@@ -94,9 +94,10 @@ int32_t kgbwt_engine_config(kgbwt_engine *e, int32_t tile_cap, int32_t tile_ctas
  *   whole batch; 0: bucket passes and tile kernels over 8-byte prefixes as in the later rounds.
  * KGBWT_OPT_LSD_BYTES (8, 12 or 16, default 16): prefix bytes that LSD round sorts (16 replaces the first rank round;
  *   the rank rounds then double from there).
- * KGBWT_OPT_CHAIN_FROM (0..64, default 1): from this rank round on, a group of two suffixes that doubling leaves
- *   together is also ordered along its repeat chain (the pairs of the two copies of a repeat, ordered where the
- *   repeat ends) instead of waiting for the doubling to reach the repeat's end; 0: never. */
+ * KGBWT_OPT_CHAIN_FROM (0..64, default 1): from this rank round on, in rounds where doubling has stalled, a group of
+ *   up to eight suffixes that doubling leaves whole is ordered along its repeat chain (the copies of a repeated
+ *   stretch move through the rounds together and are ordered where the repeat ends) instead of waiting for the
+ *   doubling to reach the repeat's end; 0: never. */
 #define KGBWT_OPT_SMALL_GROUP 1
 #define KGBWT_OPT_WARP_PATH 2
 #define KGBWT_OPT_LSD_ROUND0 3

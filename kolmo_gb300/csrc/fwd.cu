@@ -74,7 +74,7 @@ struct FwdArgs {
     u32 *lhist, *ltile, *segagg;
     u32 *lbase;  // round 0: per block and digit slot, the pass's first position of every digit
     u32 spin_limit;
-    // chains of repeat pairs (rank rounds >= chain_from): bit x of cbits = the pair of suffix x continues at x + 1;
+    // repeat chains (rank rounds >= chain_from): bit x of cbits = the group of suffix x continues at x + 1;
     // cnz / ctn: the next-zero tables over cbits' words (see k_chain_nz)
     u32 *cbits, *cnz, *ctn;
     u32 cwords, ctiles, chain_from;
@@ -818,21 +818,23 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------------ repeat chains
-// Two suffixes a and b in one group have equal first characters, so they sort as a + 1 and b + 1 do. In a repeat
-// (two equal stretches of text) the pairs {a, b}, {a + 1, b + 1}, ... are groups of two round after round until the
+// Suffixes in one group have equal first characters, so they sort among themselves as their successors (each
+// position + 1) do. Inside a repeat (equal stretches of text) the members of a group G move along together: their
+// successors fill one group G', whose successors fill one group G'', and so on, round after round, until the
 // doubling step reaches the end of the repeat, about log2(length / h) rounds later. The chain kernels order such
-// pairs in one step: for every pair {a, b} of this round's tiny list, bit a and bit b of cbits say that a + 1 and
-// b + 1 are in one group now (so a's chain continues at a + 1, whose group, if it is a pair, is {a + 1, b + 1}). The
-// first clear bit e >= a ends a's chain, and the pair sorts as the suffixes e + 1 and b + (e - a) + 1 do: by their
-// current ranks when those differ, the shorter first when one of them lies past the block end, else not yet.
-// (Each id has one partner, so chains of different pairs never overlap inconsistently: the chain from a would have
-// to pass through b's own group to meet b's chain, and b's group is {a, b}.)
+// groups in one step. For every tiny group of this round whose members' successors all lie in one group, each
+// member's bit in cbits is set (x's chain continues at x + 1). The first clear bit e >= x1 (x1: any member) ends the
+// chain: the members x_i sort as the suffixes x_i + (e - x1) + 1 do, by their current ranks, a suffix past the block
+// end first (at most one member's can be: they are distinct positions inside the block). The successor sets along
+// the chain are contained in single groups, so every member's chain has the same length. The step runs only where
+// doubling has stalled (the round follows one that finished less than a fifth of its actives): earlier, common short
+// phrases put most chains through groups whose other members leave the repeat, and the chains end undecided.
 constexpr u32 NZ_TILE = 4096;  // words per tile of the next-zero table
 constexpr u32 NZ_NONE = 0xFFFFFFFFu;
 
 __device__ __forceinline__ bool chain_on(const FwdArgs &a) {
     const Ctl *c = a.ctl;
-    return a.chain_from && c->round >= a.chain_from && (u32)c->cnt[L_P0 + c->rpar] != 0;
+    return a.chain_from && c->round >= a.chain_from && c->chain_go && (u32)c->cnt[L_P0 + c->rpar] != 0;
 }
 
 __global__ void __launch_bounds__(TPB) k_chain_clear(FwdArgs a) {
@@ -840,7 +842,7 @@ __global__ void __launch_bounds__(TPB) k_chain_clear(FwdArgs a) {
     for (u32 w = blockIdx.x * TPB + threadIdx.x; w < a.cwords; w += gridDim.x * TPB) a.cbits[w] = 0;
 }
 
-// Bits of the pairs whose successors share a group.
+// Bits of the tiny groups whose members' successors all share one group.
 __global__ void __launch_bounds__(TPB) k_chain_link(FwdArgs a) {
     if (!chain_on(a)) return;
     const Ctl *ctl = a.ctl;
@@ -850,14 +852,29 @@ __global__ void __launch_bounds__(TPB) k_chain_link(FwdArgs a) {
     const u32 *isa = a.isa[rpar];
     for (u32 s = blockIdx.x * TPB + threadIdx.x; s < nseg; s += gridDim.x * TPB) {
         const Seg g = in.seg[s];
-        if (g.len != 2 || (u64)g.start + 2 > nslots) continue;
-        const u32 x = in.eid[g.start], y = in.eid[g.start + 1];
+        const u32 len = g.len;
+        if (len < 2 || len > GTINY || (u64)g.start + len > nslots) continue;
         const u64 end = blk_end(a, seg_blk(g.bd));
-        if ((u64)x + 1 >= end || (u64)y + 1 >= end) continue;
-        if (__ldg(isa + x + 1) != __ldg(isa + y + 1)) continue;
-        if (KGB_OK((x >> 5) < a.cwords && (y >> 5) < a.cwords, &a.ctl->err, E_RANK)) {
-            atomicOr(a.cbits + (x >> 5), 1u << (x & 31));
-            atomicOr(a.cbits + (y >> 5), 1u << (y & 31));
+        u32 v[GTINY];
+        bool ok = true;
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            v[q] = q < len ? in.eid[g.start + q] : 0u;
+            if (q < len && (u64)v[q] + 1 >= end) ok = false;
+        }
+        if (!ok) continue;
+        u32 r0 = 0;
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            if (q >= len) break;
+            const u32 r = __ldg(isa + v[q] + 1);
+            if (q == 0) r0 = r; else ok = ok && r == r0;
+        }
+        if (!ok) continue;
+#pragma unroll
+        for (u32 q = 0; q < GTINY; q++) {
+            if (q >= len) break;
+            if (KGB_OK((v[q] >> 5) < a.cwords, &a.ctl->err, E_RANK)) atomicOr(a.cbits + (v[q] >> 5), 1u << (v[q] & 31));
         }
     }
 }
@@ -935,15 +952,11 @@ __device__ __forceinline__ u32 chain_end(const FwdArgs &a, u32 x) {
     return (w2 << 5) + __ffs(~a.cbits[w2]) - 1;
 }
 
-// The order of the pair {x, y} (one group, this round's ranks isa) from x's chain: -1 when x sorts first, 1 when y
-// does, 0 when the chain ends in a larger group (not decided yet).
-__device__ __forceinline__ int chain_order(const FwdArgs &a, const u32 *__restrict__ isa, u32 x, u32 y, u64 end) {
-    const u32 e = chain_end(a, x);
-    const u64 f = (u64)e + 1, g = (u64)y + (e - x) + 1;
-    if (f >= end) return -1;  // x's side reaches the block end first: the shorter suffix sorts first
-    if (g >= end) return 1;
-    const u32 rf = __ldg(isa + f), rg = __ldg(isa + g);
-    return rf == rg ? 0 : (rf < rg ? -1 : 1);
+// The chain key of member x of a group whose chain has length d (this round's ranks isa): 0 for a suffix whose
+// position x + d + 1 lies past the block end (the shorter suffix sorts first), else 1 + the rank there.
+__device__ __forceinline__ u32 chain_key(const u32 *__restrict__ isa, u32 x, u32 d, u64 end) {
+    const u64 f = (u64)x + d + 1;
+    return f >= end ? 0u : __ldg(isa + f) + 1u;
 }
 
 // ------------------------------------------------------------------------------------------------ tiny groups
@@ -993,10 +1006,15 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? ids[g.start + q] : 0u;
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++) k[q] = q < len ? rank_key(isa_cur, v[q], h, end) : 0xFFFFFFFFu;
-        if (len == 2 && k[0] == k[1] && chain_on(a)) {
-            // a pair that doubling leaves together: its repeat chain may order it now
-            const int o = chain_order(a, isa_cur, v[0], v[1], end);
-            if (o) { k[0] = o < 0 ? 0u : 1u; k[1] = o < 0 ? 1u : 0u; }
+        bool same = len >= 2;
+#pragma unroll
+        for (u32 q = 1; q < GTINY; q++) same = same && (q >= len || k[q] == k[0]);
+        if (same && chain_on(a)) {
+            // a group that doubling leaves whole: its repeat chain may order it now
+            const u32 d = chain_end(a, v[0]) - v[0];
+#pragma unroll
+            for (u32 q = 0; q < GTINY; q++)
+                if (q < len) k[q] = chain_key(isa_cur, v[q], d, end);
         }
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
         if (mlen <= 2) {
@@ -1685,6 +1703,11 @@ __global__ void k_ctl_round_end(FwdArgs a) {
     c->rpar = rp ^ 1;
     c->round += 1;
     c->h = c->round == 1 ? c->h0 : c->h * 2;
+    // repeat chains pay off once doubling stalls: the next round follows them when this one left at least four
+    // fifths of its actives unfinished (round 0 counts every suffix as active)
+    const u32 prev = c->round == 1 ? c->m : c->prev_active;
+    c->chain_go = (u64)active * 5 >= (u64)prev * 4;
+    c->prev_active = active;
     c->pass = 0;
     u32 cont = active > 0;
     if (cont && c->round > c->maxrounds) { c->err |= 1; cont = 0; }
@@ -2216,7 +2239,8 @@ static cudaError_t enq_lsd_sort_seg(Launcher &L, const FwdArgs &a, u32 slots, u3
 static u32 host_active_slots(const Ctl &c) { return c.lsd_act; }
 
 // The repeat-chain tables of a rank round (each kernel returns at once before round chain_from or on an empty tiny
-// list): clear the bits, set them for the linked pairs, build the next-zero tables.
+// list, and in rounds where doubling has not stalled): clear the bits, set them for the linked tiny groups, build the
+// next-zero tables.
 static cudaError_t enq_chain(Launcher &L, const FwdArgs &a, u32 elems, u32 segs) {
     cudaError_t e;
     L.tag(K_CHAIN, elems, segs);
@@ -2313,7 +2337,8 @@ int FwdEngine::run_plain(cudaStream_t s) {
                 KGB_CHECK(L.go(k_group_warp, grid_scan, TPB, 0, a));
             }
             if (!prefix && cnt_e(L_P0 + rp)) {
-                if (a.chain_from && (u32)round >= a.chain_from) KGB_CHECK(enq_chain(L, a, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp)));
+                if (a.chain_from && (u32)round >= a.chain_from && h_ctl->chain_go)
+                    KGB_CHECK(enq_chain(L, a, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp)));
                 L.tag(K_GROUP, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
                 KGB_CHECK(L.go(k_group_thread, grid_msd, TPB, 0, a));
             }

@@ -62,6 +62,8 @@ struct Ctl {
     u32 seq;            // call sequence number (tags the look-back words of the radix passes)
     u32 p_alloc;        // slots taken so far in the tiny-group id array (shared by both parities, never reused)
     u32 idn;            // suffix ids of the batch lie in [0, idn) (the rank buffers' used extent)
+    u32 prev_active;    // active suffixes of the round that just ended (the round-end kernel's last count)
+    u32 chain_go;       // this round follows repeat chains (doubling split less than a fifth of the actives)
 };
 
 struct FwdConfig {
@@ -72,7 +74,7 @@ struct FwdConfig {
     int warp_path = 1;    // tiles whose groups are all <= 32 long go to the warp-level kernel
     int lsd_round0 = 1;   // round 0 as one LSD radix sort of all suffixes; 0: bucket passes + tiles over 8-byte prefixes
     int lsd_bytes = 16;   // prefix bytes the LSD round 0 sorts (8, 12 or 16)
-    int chain_from = 1;   // first rank round whose pairs are also ordered along their repeat chains (0: never)
+    int chain_from = 1;   // first rank round whose tiny groups may be ordered along their repeat chains (0: never)
 };
 // Fields of FwdConfig a caller set explicitly (they override the tuning table).
 enum : u32 {
