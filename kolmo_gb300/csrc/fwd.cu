@@ -829,6 +829,27 @@ __global__ void __launch_bounds__(TPB, 3) k_tile_warp(FwdArgs a) {
 // the chain are contained in single groups, so every member's chain has the same length. The step runs only where
 // doubling has stalled (the round follows one that finished less than a fifth of its actives): earlier, common short
 // phrases put most chains through groups whose other members leave the repeat, and the chains end undecided.
+// Exclusive suffix minimum over the threads of a CTA of NT threads: thread i gets min(v_j, j > i) (0xFFFFFFFF for the
+// last). sm holds NT / 32 words; the call synchronises the CTA and leaves sm free for reuse.
+template <int NT>
+__device__ __forceinline__ u32 block_suffix_min_excl(u32 v, u32 *sm) {
+    const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 incl = v;  // inclusive suffix minimum within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_down_sync(0xffffffffu, incl, o);
+        if (lane + o < 32) incl = min(incl, t);
+    }
+    if (lane == 0) sm[warp] = incl;  // the warp's minimum
+    __syncthreads();
+    u32 later = 0xFFFFFFFFu;  // minimum of the later warps
+    for (u32 w = warp + 1; w < (u32)(NT / 32); w++) later = min(later, sm[w]);
+    u32 excl = __shfl_down_sync(0xffffffffu, incl, 1);
+    if (lane == 31) excl = 0xFFFFFFFFu;
+    __syncthreads();
+    return min(excl, later);
+}
+
 constexpr u32 NZ_TILE = 4096;  // words per tile of the next-zero table
 constexpr u32 NZ_NONE = 0xFFFFFFFFu;
 
@@ -883,7 +904,7 @@ __global__ void __launch_bounds__(TPB) k_chain_link(FwdArgs a) {
 // clear bit (NZ_NONE if none), and per tile the first such word (ctn, NZ_NONE if none). One CTA per tile.
 __global__ void __launch_bounds__(TPB) k_chain_nz(FwdArgs a) {
     if (!chain_on(a)) return;
-    __shared__ u32 sm[TPB];
+    __shared__ u32 sm[TPB / 32];
     constexpr u32 PER = NZ_TILE / TPB;
     for (u32 t = blockIdx.x; t < a.ctiles; t += gridDim.x) {
         const u32 w0 = t * NZ_TILE + threadIdx.x * PER;
@@ -895,13 +916,9 @@ __global__ void __launch_bounds__(TPB) k_chain_nz(FwdArgs a) {
             if (w < a.cwords && a.cbits[w] != 0xFFFFFFFFu) nxt = w;
             loc[q] = nxt;
         }
-        sm[threadIdx.x] = nxt;  // this thread's first such word
-        __syncthreads();
-        // the first such word after this thread's run: the minimum over the later threads' runs
-        u32 after = NZ_NONE;
-        for (u32 j = threadIdx.x + 1; j < TPB; j++) {
-            if (sm[j] != NZ_NONE) { after = sm[j]; break; }
-        }
+        // the first such word after this thread's run: the minimum over the later threads' runs (words grow with the
+        // thread index and NZ_NONE is the largest value)
+        const u32 after = block_suffix_min_excl<TPB>(nxt, sm);
 #pragma unroll
         for (int q = 0; q < (int)PER; q++) {
             const u32 w = w0 + q;
@@ -916,7 +933,7 @@ __global__ void __launch_bounds__(TPB) k_chain_nz(FwdArgs a) {
 // minimum over the tiles); ctn[ctiles] is the last word, which is never set.
 __global__ void __launch_bounds__(1024) k_chain_tiles(FwdArgs a) {
     if (!chain_on(a)) return;
-    __shared__ u32 sm[1024];
+    __shared__ u32 sm[1024 / 32];
     const u32 nt = a.ctiles;
     const u32 per = (nt + 1023) / 1024;
     const u32 t0 = threadIdx.x * per;
@@ -925,12 +942,8 @@ __global__ void __launch_bounds__(1024) k_chain_tiles(FwdArgs a) {
         const u32 t = t0 + q;
         if (t < nt && a.ctn[t] != NZ_NONE) nxt = a.ctn[t];
     }
-    sm[threadIdx.x] = nxt;
-    __syncthreads();
-    u32 after = a.cwords - 1;
-    for (u32 j = threadIdx.x + 1; j < 1024; j++) {
-        if (sm[j] != NZ_NONE) { after = sm[j]; break; }
-    }
+    u32 after = block_suffix_min_excl<1024>(nxt, sm);
+    if (after == NZ_NONE) after = a.cwords - 1;
     for (int q = (int)per - 1; q >= 0; q--) {
         const u32 t = t0 + q;
         if (t < nt) {
@@ -1004,18 +1017,16 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         u32 k[GTINY], v[GTINY];
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? ids[g.start + q] : 0u;
+        // In a round that follows repeat chains, a group whose chain is at least h long would come out of doubling
+        // whole (its members' positions + h share one group); its chain key, the rank d + 1 positions on, orders it
+        // at least as far, so it takes that key instead (one gather per member either way). Shorter chains, and
+        // rounds without chains, take the doubling key.
+        u32 d = 0;
+        if (len >= 2 && chain_on(a)) d = chain_end(a, v[0]) - v[0];
+        const bool by_chain = d >= h;
 #pragma unroll
-        for (u32 q = 0; q < GTINY; q++) k[q] = q < len ? rank_key(isa_cur, v[q], h, end) : 0xFFFFFFFFu;
-        bool same = len >= 2;
-#pragma unroll
-        for (u32 q = 1; q < GTINY; q++) same = same && (q >= len || k[q] == k[0]);
-        if (same && chain_on(a)) {
-            // a group that doubling leaves whole: its repeat chain may order it now
-            const u32 d = chain_end(a, v[0]) - v[0];
-#pragma unroll
-            for (u32 q = 0; q < GTINY; q++)
-                if (q < len) k[q] = chain_key(isa_cur, v[q], d, end);
-        }
+        for (u32 q = 0; q < GTINY; q++)
+            k[q] = q >= len ? 0xFFFFFFFFu : by_chain ? chain_key(isa_cur, v[q], d, end) : rank_key(isa_cur, v[q], h, end);
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
         if (mlen <= 2) {
             KGB_CS(0, 1);
