@@ -18,6 +18,7 @@ struct InvBlock {
     u32 hmask;       // 2^k - 1 with 2^k >= n
     u32 hmul;        // odd multiplier: the top k bits of 2^64 / golden ratio (rows of the marks are a Weyl sequence)
     u32 hinv;        // hmul^-1 mod 2^32: row q is mark (q * hinv) & hmask
+    u32 qbase;       // the block's chains in the walk's sequence over all blocks: qbase .. qbase + nreg
 };
 
 struct InvStats {
@@ -56,7 +57,9 @@ class InvEngine {
     u64 Ncap = 0, Tcap = 0, Ccap = 0;
     u32 Bcap = 0;
     u64 N = 0, nchunk_all = 0, nchains = 0;
-    u32 B = 0, maxchains = 0, njump = 0, nchunks = 0;
+    u32 B = 0, maxchains = 0, njump = 0, nchunks = 0, nwalk = 0;
+    int walk_grid = 0;   // resident CTAs of the persistent walk kernel
+    bool small = false;  // a small batch: denser marks and the persistent walk
     std::vector<u32> h_off;
     std::vector<InvBlock> h_blk;
     std::vector<u32> h_chunks;  // (block, first chain, end chain) triples for the walk
@@ -79,9 +82,10 @@ class InvEngine {
         u64 N, Ncap, nchunk_all, nchains;
         u32 B, njump, nchunks;
         const void *U, *out;
+        bool small;
         bool operator==(const GraphKey &o) const {
             return N == o.N && Ncap == o.Ncap && nchunk_all == o.nchunk_all && nchains == o.nchains && B == o.B &&
-                   njump == o.njump && nchunks == o.nchunks && U == o.U && out == o.out;
+                   njump == o.njump && nchunks == o.nchunks && U == o.U && out == o.out && small == o.small;
         }
     };
     GraphKey graph_key{}, seen_key{};
