@@ -27,7 +27,7 @@ const char *kernel_name(int k) {
         "tile_warp_prefix", "tile_warp_prefix_keyed", "tile_warp_rank", "tile_warp_rank_keyed",
         "lsd_begin", "lsd_key0", "lsd_hist", "lsd_pass", "seg_count", "seg_scan", "seg_emit1", "seg_emit2",
         "group_thread", "group_warp", "mkeys", "lsd_ident", "seg_rank",
-        "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit", "chain", "tkeys"};
+        "inv_chunkhist", "inv_chunkscan", "inv_scatter", "inv_walk", "inv_rank_init", "inv_jump", "inv_emit", "chain"};
     return k >= 0 && k < K_NKERNELS ? names[k] : "?";
 }
 

@@ -122,7 +122,7 @@ enum KernelId : int {
     K_TILE_RANK, K_TILE_RANK_KEYED, K_CTL, K_SAMPLES,
     K_WARP_PREFIX, K_WARP_PREFIX_KEYED, K_WARP_RANK, K_WARP_RANK_KEYED,
     K_LSD_BEGIN, K_LSD_KEY0, K_LSD_HIST, K_LSD_PASS, K_SEG_COUNT, K_SEG_SCAN, K_SEG_EMIT1, K_SEG_EMIT2, K_GROUP, K_GROUP_WARP, K_MKEYS, K_LSD_IDENT, K_SEG_RANK,
-    K_INV_TILEHIST, K_INV_COLSCAN, K_INV_SCATTER, K_INV_WALK, K_INV_RANKINIT, K_INV_JUMP, K_INV_EMIT, K_CHAIN, K_TKEYS, K_NKERNELS
+    K_INV_TILEHIST, K_INV_COLSCAN, K_INV_SCATTER, K_INV_WALK, K_INV_RANKINIT, K_INV_JUMP, K_INV_EMIT, K_CHAIN, K_NKERNELS
 };
 const char *kernel_name(int k);
 

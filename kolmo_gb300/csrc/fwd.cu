@@ -987,31 +987,6 @@ __device__ __forceinline__ void cswap(u32 &ka, u32 &va, u32 &kb, u32 &vb) {
 }
 #define KGB_CS(i, j) cswap(k[i], v[i], k[j], v[j])
 
-// Raw keys of the tiny groups, gathered ahead: tkey[x] = ISA[id + h] for every slot x of the tiny-group id array
-// (clamped into the rank buffer; k_group_thread corrects members whose position + h lies past their block), with
-// every load independent, so that k_group_thread's chain of dependent loads (descriptor, ids, ranks) loses a link.
-// It runs where at least half of the slots belong to this round's groups (the others are finished suffixes, whose
-// gathers are wasted) and in rounds without repeat chains (which take other keys); the scratch is the second
-// bucket-pass list's key array, free once the round's bucket passes are done.
-__device__ __forceinline__ bool tkeys_on(const FwdArgs &a) {
-    const Ctl *c = a.ctl;
-    const u32 live = (u32)c->cnt[L_P0 + c->rpar];
-    return live && (u64)live * 2 >= c->p_alloc && !chain_on(a);
-}
-
-__global__ void __launch_bounds__(TPB) k_tkeys(FwdArgs a) {
-    if (!tkeys_on(a)) return;
-    const Ctl *ctl = a.ctl;
-    const u32 rpar = ctl->rpar, h = ctl->h;
-    const u32 *ids = a.lists[L_P0 + rpar].eid, *isa = a.isa[rpar];
-    const u32 ns = min(ctl->p_alloc, (u32)a.cap_n);
-    u32 *tk = a.lhi[1];
-    for (u32 x = blockIdx.x * TPB + threadIdx.x; x < ns; x += gridDim.x * TPB) {
-        const u64 j = (u64)__ldcs(ids + x) + h;
-        __stcs(tk + x, j < a.cap_n ? __ldg(isa + j) : 0u);
-    }
-}
-
 __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
     const Ctl *ctl = a.ctl;
     const u32 rpar = ctl->rpar, h = ctl->h;
@@ -1027,8 +1002,6 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
     u32 *isa_nxt = a.isa[rpar ^ 1];
     u32 *ids = in.eid;
     const u32 lane = lane_id();
-    const bool pre = tkeys_on(a);  // the raw keys were gathered ahead (k_tkeys)
-    const u32 *tk = a.lhi[1];
     for (u32 base = blockIdx.x * TPB; base < nseg; base += gridDim.x * TPB) {
         const u32 s = base + threadIdx.x;
         const bool ok = s < nseg;
@@ -1052,13 +1025,8 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         if (len >= 2 && chain_on(a)) d = chain_end(a, v[0]) - v[0];
         const bool by_chain = d >= h;
 #pragma unroll
-        for (u32 q = 0; q < GTINY; q++) {
-            if (q >= len) { k[q] = 0xFFFFFFFFu; continue; }
-            if (by_chain) { k[q] = chain_key(isa_cur, v[q], d, end); continue; }
-            if (!pre) { k[q] = rank_key(isa_cur, v[q], h, end); continue; }
-            const u32 dd = (u32)(end - v[q]);  // the gathered raw key, or the past-the-end key of rank_key
-            k[q] = h < dd ? tk[g.start + q] + h : dd - 1;
-        }
+        for (u32 q = 0; q < GTINY; q++)
+            k[q] = q >= len ? 0xFFFFFFFFu : by_chain ? chain_key(isa_cur, v[q], d, end) : rank_key(isa_cur, v[q], h, end);
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
         if (mlen <= 2) {
             KGB_CS(0, 1);
@@ -2382,8 +2350,6 @@ int FwdEngine::run_plain(cudaStream_t s) {
             if (!prefix && cnt_e(L_P0 + rp)) {
                 if (a.chain_from && (u32)round >= a.chain_from && h_ctl->chain_go)
                     KGB_CHECK(enq_chain(L, a, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp)));
-                L.tag(K_TKEYS, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
-                KGB_CHECK(L.go(k_tkeys, grid_msd, TPB, 0, a));
                 L.tag(K_GROUP, cnt_e(L_P0 + rp), cnt_s(L_P0 + rp));
                 KGB_CHECK(L.go(k_group_thread, grid_msd, TPB, 0, a));
             }
@@ -2470,7 +2436,6 @@ static int add_tile_round(cudaStream_t s, cudaGraph_t g, Deps &deps, Launcher &L
         if ((e = L.go(k_mkeys, L.grid_msd, TPB, 0, a))) return e;
         if ((e = L.go(k_group_warp, L.grid_scan, TPB, 0, a))) return e;
         if (a.chain_from && (e = enq_chain(L, a, 0, 0))) return e;
-        if ((e = L.go(k_tkeys, L.grid_msd, TPB, 0, a))) return e;
         return L.go(k_group_thread, L.grid_msd, TPB, 0, a);
     });
 }

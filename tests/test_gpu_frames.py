@@ -20,6 +20,7 @@ import os
 import random
 import struct
 import subprocess
+import time
 
 import numpy as np
 import pytest
@@ -159,3 +160,32 @@ def test_reference_release_frames_decode(clis, tmp_path):
         decoded += 1
     assert decoded >= 50
     assert log.calls("inv") > 0, "no frame of the corpus reached the GPU inverse"
+
+
+def test_whole_frame_throughput(clis, tmp_path):
+    """Whole -8 frames of a 256 MiB prose file (eight 32 MiB blocks, every host thread): the GPU CLI's frame equals
+    the reference CLI's, and both decode it back. Prints the two CLIs' compress and decompress throughput (MiB/s of
+    input, process start and the GPU's context creation included): LZP, QLFC and the container stay on the host
+    cores in both, so this is the whole codec's speed, not the sorter's."""
+    ref, gpu = clis
+    log = GpuLog(tmp_path)
+    T = W.zipf_prose(256 << 20, 2561)
+    p = str(tmp_path / "prose256")
+    T.tofile(p)
+    t = str(os.cpu_count() or 1)
+    res = {}
+    for name, cli, env in (("reference", ref, None), ("gpu", gpu, log.env)):
+        z, back = p + f".{name}.k", p + f".{name}.back"
+        t0 = time.perf_counter()
+        _run([cli, "-8", "-f", "-T", t, p, "-o", z], env)
+        t1 = time.perf_counter()
+        _run([cli, "-d", "-f", "-T", t, z, "-o", back], env)
+        t2 = time.perf_counter()
+        assert np.array_equal(np.fromfile(back, np.uint8), T), name
+        res[name] = (T.size / 2**20 / (t1 - t0), T.size / 2**20 / (t2 - t1))
+    assert open(p + ".reference.k", "rb").read() == open(p + ".gpu.k", "rb").read()
+    assert log.calls("fwd") >= 8 and log.calls("inv") >= 8
+    batches = [x for x in log.lines() if x.startswith("fwd")]
+    print(f"\nwhole -8 frames, 256 MiB prose, -T {t}: reference CLI compress {res['reference'][0]:.1f} MiB/s, "
+          f"decompress {res['reference'][1]:.1f} MiB/s; GPU CLI compress {res['gpu'][0]:.1f} MiB/s, decompress "
+          f"{res['gpu'][1]:.1f} MiB/s; {log.calls('fwd')} forward calls in {len(batches)} batches")
