@@ -80,6 +80,7 @@ struct FwdArgs {
     u32 cwords, ctiles, chain_from;
     // capacities (checked build): elements / text bytes, small and large segment records, tile-map entries
     u64 cap_n, cap_segs, cap_segk, cap_segl, cap_segt, cap_segm, cap_tms, cap_tml;
+    u32 cap_res;  // entries of each resolved list
 };
 
 // device error bits
@@ -115,18 +116,19 @@ __device__ __forceinline__ u32 rank_key(const u32 *__restrict__ isa, u32 i, u32 
 }
 
 // The final state of a suffix: rank = suffix-array position p (block-local), L column row p + 1 = T[i - 1]
-// (the sentinel row's byte value is never read), optional suffix array, and its index in the resolved list.
+// (the sentinel row's byte value is never read), optional suffix array, and its index in the resolved list. The
+// resolved list holds cap_res entries, a sixteenth of the ids: the next round's fixup scatters the list only when a
+// round finished at most that many suffixes and copies the whole rank buffer otherwise, so entries past the
+// capacity are counted but never needed.
 // As resolve, with the block's descriptor and the L-column byte (T[id - 1], 0 for the block's first suffix) already
 // loaded: callers load the bytes of several finished suffixes at once.
 __device__ __forceinline__ void resolve_byte(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, const BlockInfo &B,
                                              ListView res, u32 ridx, u8 byte) {
-    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
-        return;
+    if (!KGB_OK(id < a.cap_n && p < B.n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK)) return;
     isa_nxt[id] = p;
     a.L[(u64)B.off + b + p + 1] = byte;
     if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
-    res.eid[ridx] = id;
-    res.ekey[ridx] = p;
+    if (ridx < a.cap_res) { res.eid[ridx] = id; res.ekey[ridx] = p; }
 }
 // As resolve, for round 0: no resolved-list entry (round 1's fixup copies the whole rank buffer) and the rank only
 // when the caller writes it.
@@ -140,13 +142,11 @@ __device__ __forceinline__ void resolve_round0(const FwdArgs &a, u32 *isa_nxt, u
 __device__ __forceinline__ void resolve(const FwdArgs &a, u32 *isa_nxt, u32 id, u32 p, u32 b, ListView res,
                                         u32 ridx) {
     BlockInfo B = a.blk[b];
-    if (!KGB_OK(id < a.cap_n && p < B.n && ridx < a.cap_n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK))
-        return;
+    if (!KGB_OK(id < a.cap_n && p < B.n && id >= B.off && id - B.off < B.n, &a.ctl->err, E_RANK)) return;
     isa_nxt[id] = p;
     a.L[(u64)B.off + b + p + 1] = id == B.off ? 0 : __ldg(a.T + id - 1);
     if (a.SA) a.SA[(u64)B.off + p] = id - B.off;
-    res.eid[ridx] = id;
-    res.ekey[ridx] = p;
+    if (ridx < a.cap_res) { res.eid[ridx] = id; res.ekey[ridx] = p; }
 }
 
 // Tiny groups keep their ids in one array for the whole sort (a tiny group only shrinks, so its members never move to
@@ -1673,7 +1673,8 @@ __global__ void __launch_bounds__(TPB) k_fixup(FwdArgs a) {
         for (u32 i = n4 * 4 + blockIdx.x * TPB + threadIdx.x; i < idn; i += stride) nxt[i] = a.isa[rpar][i];
         return;
     }
-    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < n; i += stride) nxt[r.eid[i]] = r.ekey[i];
+    const u32 nl = min(n, a.cap_res);  // n <= idn / 16 < cap_res here: the list holds every entry
+    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < nl; i += stride) nxt[r.eid[i]] = r.ekey[i];
 }
 
 // ------------------------------------------------------------------------------------------------ control
@@ -1794,16 +1795,19 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_isa[0], n * 4);
     add((void **)&d_isa[1], n * 4);
     add((void **)&d_blk, (size_t)bcap * sizeof(BlockInfo));
+    const u64 nres = n / 16 + 64;  // resolved-list entries (see resolve)
     for (int l = 0; l < NLISTS; l++) {
-        if (l != L_P1) add((void **)&lists[l].eid, n * 4);  // the two tiny lists share one id array
         const bool small = l == L_S0 || l == L_S1 || l == L_KS;
         const bool res = l == L_R0 || l == L_R1;
         const bool tiny = l == L_P0 || l == L_P1, med = l == L_M0 || l == L_M1;
+        if (l != L_P1) add((void **)&lists[l].eid, (res ? nres : n) * 4);  // the two tiny lists share one id array
         if (tiny || med) {  // ids and segment descriptors only
             add((void **)&lists[l].seg, (tiny ? nseg_small : nseg_med) * sizeof(Seg));
             continue;
         }
-        if (l != L_S0 && l != L_S1) add((void **)&lists[l].ekey, n * 4);
+        // keys: the large lists share one array (only the round's input list carries keys, from its key generation
+        // on); the small lists have none
+        if (l != L_S0 && l != L_S1 && l != L_L1) add((void **)&lists[l].ekey, (res ? nres : n) * 4);
         if (!res) {
             add((void **)&lists[l].seg, (l == L_KS ? nseg_small : small ? nseg_s : nseg_large) * sizeof(Seg));
             add((void **)&lists[l].tmap, (small ? ntm_small : ntm_large) * 4);
@@ -1878,6 +1882,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     size_t off = 0;
     for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
     lists[L_P1].eid = lists[L_P0].eid;
+    lists[L_L1].ekey = lists[L_L0].ekey;
     d_lval[0] = lists[L_K0].eid; d_lval[1] = lists[L_K0].ekey;
     d_lhi[0] = lists[L_K1].eid; d_lhi[1] = lists[L_K1].ekey;
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
@@ -1929,6 +1934,7 @@ void FwdEngine::set_caps(FwdArgs &a) const {
     a.cap_segm = cap_segm;
     a.cap_tms = cap_tms;
     a.cap_tml = cap_tml;
+    a.cap_res = (u32)(Ncap / 16 + 64);
 }
 
 int FwdEngine::plan(const u32 *n, const u32 *r, int count, bool want_sa) {
