@@ -14,11 +14,8 @@ the same objects with ``libkgbwt.so`` linked in place of ``sais.c`` (the only ca
 * frames written by reference releases (tests/v12/*.kolmo) decode to the originals' digests (tests/v12.sha256).
 
 ``KGBWT_STATS`` makes the GPU library log its batches, which shows that the block sorts ran on the GPU."""
-import ast
 import hashlib
 import os
-import random
-import struct
 import subprocess
 import time
 
@@ -26,6 +23,7 @@ import numpy as np
 import pytest
 
 import stage_ref
+from frame_inputs import determinism_inputs, expected_digests
 from kolmo_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -69,32 +67,12 @@ class GpuLog:
         return sum(int(x.split()[1].split("=")[1]) for x in self.lines() if x.startswith(kind))
 
 
-def _determinism_inputs():
-    """The inputs of the reference's determinism check: its `inputs()` generator, taken from the staged
-    benchmark/determinism/check.py and run here (the module itself runs the check on import)."""
-    path = os.path.join(TREE, "benchmark", "determinism", "check.py")
-    tree = ast.parse(open(path).read(), path)
-    fn = next(n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == "inputs")
-    ns = {"random": random, "struct": struct}
-    exec(compile(ast.Module(body=[fn], type_ignores=[]), path, "exec"), ns)
-    return [(name, data) for name, data, _ in ns["inputs"]()]
-
-
-def _expected_digests():
-    out = {}
-    for line in open(os.path.join(TREE, "benchmark", "determinism", "expected.sha256")):
-        parts = line.rstrip("\n").split("  ")
-        if len(parts) == 3:
-            out[(parts[1], parts[2])] = parts[0]
-    return out
-
-
 def test_determinism_digests_at_levels_8_and_9(clis, tmp_path):
     _, gpu = clis
     log = GpuLog(tmp_path)
-    want = _expected_digests()
+    want = expected_digests(TREE)
     checked = 0
-    inputs = _determinism_inputs()
+    inputs = determinism_inputs(TREE)
     for name, data in inputs:
         p = str(tmp_path / name)
         open(p, "wb").write(data)
