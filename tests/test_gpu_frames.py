@@ -118,6 +118,40 @@ def test_frames_equal_reference_cli(clis, tmp_path):
                     assert np.array_equal(np.fromfile(back, np.uint8), T), (name, level, t, dec)
 
 
+def test_corrupted_frames_fail_alike(clis, tmp_path):
+    """On a string that is no BWT for its primary index the reference's decoders emit bytes that the block checksum
+    rejects, where the GPU inverse returns -1, which the codec maps to KB_DATA_CORRUPT (src/codecs/bwt_stream.c:294).
+    At the frame level the outcome must be the same: for single-byte corruptions throughout a -8 frame, both CLIs
+    reject the same frames, and where both decode, they decode the same bytes."""
+    ref, gpu = clis
+    log = GpuLog(tmp_path)
+    T = W.markov2(1 << 20, 0xBAD)
+    p = str(tmp_path / "m1")
+    T.tofile(p)
+    z = p + ".k"
+    _run([ref, "-8", "-f", p, "-o", z])
+    frame = bytearray(open(z, "rb").read())
+    rng = np.random.default_rng(31)
+    positions = sorted(set(int(x) for x in rng.integers(0, len(frame), 24)) | set(range(16, 80, 4)))
+    rejected = 0
+    for pos in positions:
+        bad = bytearray(frame)
+        bad[pos] ^= 0x5A
+        zb, outs = str(tmp_path / "bad.k"), {}
+        open(zb, "wb").write(bytes(bad))
+        for name, cli, env in (("reference", ref, None), ("gpu", gpu, log.env)):
+            out = str(tmp_path / f"bad.{name}")
+            if os.path.exists(out):
+                os.remove(out)
+            r = subprocess.run([cli, "-d", "-f", zb, "-o", out], capture_output=True, env=env)
+            outs[name] = (r.returncode != 0, open(out, "rb").read() if r.returncode == 0 else None)
+        assert outs["reference"][0] == outs["gpu"][0], (pos, outs["reference"][0], outs["gpu"][0])
+        assert outs["reference"][1] == outs["gpu"][1], pos
+        rejected += outs["reference"][0]
+    assert rejected > 0
+    print(f"\n{rejected} of {len(positions)} single-byte corruptions rejected by both CLIs")
+
+
 def test_reference_release_frames_decode(clis, tmp_path):
     _, gpu = clis
     log = GpuLog(tmp_path)
