@@ -1,6 +1,9 @@
 """Concurrent drop-in calls: the reference's block workers call the sorter from one thread per block
 (src/core/blocks.c:181, src/core/compress.c:221, src/core/decode.c:405). Calls that arrive while the device worker is
 busy are coalesced into one batch, and each call still gets the bytes it would get alone (the oracle's)."""
+import os
+import subprocess
+import sys
 import threading
 
 import numpy as np
@@ -75,3 +78,37 @@ def test_concurrent_calls_keep_their_own_return_codes():
     assert res[0][0] == 0 and np.array_equal(res[0][1], T)
     assert res[2][0] == 0 and np.array_equal(res[2][1], T)
     assert res[1][0] == -1 and res[3][0] == -1
+
+
+_CAPPED = r"""
+import sys, threading
+import numpy as np
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/oracle")
+import oracle as O
+from kolmo_gb300 import codec
+from kolmo_gb300 import workloads as W
+blocks = [W.markov2(1 << 20, 300 + i) for i in range(8)]
+want = [O.bwt_aux(T, 1 << 17) for T in blocks]
+codec.bwt_aux(blocks[0], 1 << 17)  # the workspace exists: the timed calls queue behind short batches
+gate = threading.Barrier(len(blocks)); res = [None] * len(blocks)
+def work(i):
+    gate.wait(); res[i] = codec.bwt_aux(blocks[i], 1 << 17)
+th = [threading.Thread(target=work, args=(i,)) for i in range(len(blocks))]
+[t.start() for t in th]; [t.join() for t in th]
+for (rc, U, I), (orc, oU, oI) in zip(res, want):
+    assert rc == 0 and np.array_equal(U, oU) and np.array_equal(I, oI)
+st = codec.dropin_stats()
+print(st["fwd_calls"], st["fwd_batches"], st["fwd_largest"])
+"""
+
+
+def test_batch_cap_bounds_coalesced_batches():
+    """KGBWT_BATCH_MIB caps a coalesced batch's input: with a 2 MiB cap, concurrent 1 MiB calls are batched at most
+    two at a time, and every call still gets the oracle's bytes (a fresh process, so the cap applies from its first
+    call)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, KGBWT_BATCH_MIB="2")
+    r = subprocess.run([sys.executable, "-c", _CAPPED, root], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    calls, batches, largest = (int(x) for x in r.stdout.split()[-3:])
+    assert calls == 9 and 1 <= largest <= 2 and batches >= 5, (calls, batches, largest)
