@@ -383,13 +383,22 @@ bool tuned_config(u64 n, FwdConfig *out) {
     return true;
 }
 
-// KGBWT_STATS=<path>: every coalesced batch appends one line (kind, calls, jobs, input bytes, return code).
-static void log_batch(int kind, size_t calls, size_t jobs, u64 bytes, int rc) {
+// KGBWT_STATS=<path>: every coalesced batch appends one line (kind, calls, jobs, input bytes, return code, and the
+// first 32 job lengths).
+static void log_batch(int kind, size_t calls, size_t jobs, u64 bytes, int rc, const std::vector<Pending *> &take) {
     static const char *path = getenv("KGBWT_STATS");
     if (!path || !*path) return;
+    std::string sizes;
+    size_t listed = 0;
+    for (const Pending *p : take) {
+        for (int32_t i = 0; i < p->count && listed < 32; i++, listed++) {
+            const int32_t n = kind ? ((const kgbwt_inv_job *)p->jobs)[i].n : ((const kgbwt_fwd_job *)p->jobs)[i].n;
+            sizes += (listed ? "," : "") + std::to_string(n);
+        }
+    }
     if (FILE *f = fopen(path, "a")) {
-        fprintf(f, "%s calls=%zu jobs=%zu bytes=%llu rc=%d\n", kind ? "inv" : "fwd", calls, jobs,
-                (unsigned long long)bytes, rc);
+        fprintf(f, "%s calls=%zu jobs=%zu bytes=%llu rc=%d sizes=%s\n", kind ? "inv" : "fwd", calls, jobs,
+                (unsigned long long)bytes, rc, sizes.c_str());
         fclose(f);
     }
 }
@@ -448,7 +457,7 @@ static void run_coalesced(Context &C, std::vector<Pending *> &take) {
             if (failed) snprintf(p->err, sizeof p->err, "%s", g_err);
         }
     }
-    log_batch(kind, take.size(), total, bytes, rc);
+    log_batch(kind, take.size(), total, bytes, rc, take);
 }
 
 // Queues one call and returns its device-level return code once a leader (possibly this thread) has run it.

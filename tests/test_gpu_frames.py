@@ -66,6 +66,14 @@ class GpuLog:
     def calls(self, kind: str) -> int:
         return sum(int(x.split()[1].split("=")[1]) for x in self.lines() if x.startswith(kind))
 
+    def sizes(self, kind: str) -> list:
+        out = []
+        for x in self.lines():
+            if x.startswith(kind):
+                field = [f for f in x.split() if f.startswith("sizes=")]
+                out += [int(v) for v in field[0][6:].split(",") if v] if field else []
+        return out
+
 
 def test_determinism_digests_at_levels_8_and_9(clis, tmp_path):
     _, gpu = clis
@@ -90,32 +98,42 @@ def test_determinism_digests_at_levels_8_and_9(clis, tmp_path):
     assert log.calls("fwd") > 0 and log.calls("inv") > 0, "no block was sorted by the GPU library"
 
 
+def _int32_walk(n_values: int, seed: int) -> np.ndarray:
+    """Binary data: a little-endian int32 random walk (the -9 planner codes a 512 KiB slice of each such block both
+    ways before it decides, src/core/blocks.c:481-517)."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.integers(-50, 50, n_values)).astype("<i4").view(np.uint8)
+
+
 def _frame_inputs():
-    return [("markov1mib", W.markov2(1 << 20, 0xC0FFEE), ("-8", "-9"), ("1",)),
-            ("prose8mib", W.zipf_prose(8 << 20, 811), ("-8", "-9"), ("1", "4")),
-            ("prose48mib", W.zipf_prose(48 << 20, 4811), ("-8",), ("4",)),  # two blocks (32 + 16 MiB) at once
-            ("acgt4mib", W.acgt(4 << 20, 77), ("-9",), ("1",)),
-            ("logs6mib", W.logs(6 << 20, 78), ("-8",), ("2",))]
+    return [("markov1mib", W.markov2(1 << 20, 0xC0FFEE), ("-8", "-9"), ("1",), []),
+            ("prose8mib", W.zipf_prose(8 << 20, 811), ("-8", "-9"), ("1", "4"), []),
+            ("prose48mib", W.zipf_prose(48 << 20, 4811), ("-8",), ("4",), []),  # two blocks (32 + 16 MiB) at once
+            ("acgt4mib", W.acgt(4 << 20, 77), ("-9",), ("1",), []),
+            ("logs6mib", W.logs(6 << 20, 78), ("-8",), ("2",), []),
+            ("int32walk96mib", _int32_walk(24 << 20, 6), ("-9",), ("8",), ["--block-size", "32"])]
 
 
 def test_frames_equal_reference_cli(clis, tmp_path):
     ref, gpu = clis
     log = GpuLog(tmp_path)
-    for name, T, levels, threads in _frame_inputs():
+    for name, T, levels, threads, extra in _frame_inputs():
         p = str(tmp_path / name)
         T.tofile(p)
         for level in levels:
             for t in threads:
                 zr, zg = p + ".ref.k", p + ".gpu.k"
-                _run([ref, level, "-f", "-T", t, p, "-o", zr])
+                _run([ref, level, "-f", "-T", t, *extra, p, "-o", zr])
                 before = log.calls("fwd")
-                _run([gpu, level, "-f", "-T", t, p, "-o", zg], log.env)
+                _run([gpu, level, "-f", "-T", t, *extra, p, "-o", zg], log.env)
                 assert log.calls("fwd") > before, (name, level, "no codec-18 block")
                 assert open(zr, "rb").read() == open(zg, "rb").read(), (name, level, t)
                 for dec, z in ((gpu, zr), (ref, zg), (gpu, zg)):
                     back = p + ".back"
                     _run([dec, "-d", "-f", z, "-o", back], log.env)
                     assert np.array_equal(np.fromfile(back, np.uint8), T), (name, level, t, dec)
+    # the -9 planner's 512 KiB slice trials of the binary blocks went through the GPU sorter too
+    assert (512 << 10) in log.sizes("fwd"), sorted(set(log.sizes("fwd")))
 
 
 def test_corrupted_frames_fail_alike(clis, tmp_path):
