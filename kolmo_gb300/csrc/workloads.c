@@ -1,6 +1,6 @@
-/* Seeded synthetic inputs for the BWT path: the block generator of the reference's own BWT tests and the
- * benchmark sources (order-2 Markov bytes, Zipf word prose with verbatim repeats, ACGT, templated log lines,
- * periodic text with flips, the Fibonacci word) plus the size distributions of the batched and serving runs.
+/* Seeded synthetic inputs for the BWT path, used by the benchmark and the autotuner: the benchmark sources (order-2
+ * Markov bytes, Zipf word prose with verbatim repeats, ACGT, templated log lines, periodic text with flips, the
+ * Fibonacci word) plus the size distributions of the batched and serving runs.
  *
  * Every generator is a pure function of its seed and produces the same bytes on x86-64 and aarch64: the only
  * floating point is IEEE double +, -, *, / and sqrt (correctly rounded on both), this file is compiled with
