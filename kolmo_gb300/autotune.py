@@ -6,8 +6,9 @@ tuning_gb300.json beside this package). Results never depend on the configuratio
 
 Tuned per bucket: CTAs per SM of the block tile kernel (tile_ctas) and of the bucket passes (msd_ctas), the
 counting-sort threshold of the tile kernel (small_group), the warp-level tile path (warp_path), the round-0 path
-(lsd_round0: one LSD radix sort of all suffixes, or bucket passes + tiles) and the prefix it sorts (lsd_bytes: 16,
-which spares the first rank round, 12 or 8). The tile capacity changes the workspace layout and is left at its default.
+(lsd_round0: one LSD radix sort of all suffixes, or bucket passes + tiles), the prefix it sorts (lsd_bytes: 16,
+which spares the first rank round, 12 or 8) and whether rank rounds follow repeat chains (chain_from: 1 or 0). The
+tile capacity changes the workspace layout and is left at its default.
 """
 from __future__ import annotations
 
@@ -42,6 +43,7 @@ CANDIDATES = {
     "tile_ctas": (2, 1),
     "small_group": (64, 0),
     "warp_path": (1, 0),
+    "chain_from": (1, 0),
 }
 
 
@@ -75,7 +77,7 @@ def _time_config(texts, cfg, reps):
     dI = torch.zeros(k, dtype=torch.int32, device="cuda")
     eng = codec.Engine()
     eng.config(0, cfg["tile_ctas"], cfg["msd_ctas"], cfg["small_group"], cfg["warp_path"], cfg["lsd_round0"],
-               cfg["lsd_bytes"])
+               cfg["lsd_bytes"], cfg["chain_from"])
     s = torch.cuda.Stream()
     times = []
     ref = None
