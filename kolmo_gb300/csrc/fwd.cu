@@ -69,7 +69,7 @@ struct FwdArgs {
     unsigned long long hcond;  // cudaGraphConditionalHandle of the loop this kernel closes (0: none)
     // round 0 as an LSD radix sort
     u32 *lval[2], *lhi[2], *segbits;
-    u32 *lkey[2];  // round 0: the 4-byte key groups carried with the ids
+    unsigned long long *lit[2];  // round 0: (key group << 32 | id) items, aliasing lval[q] and lhi[q]
     u64 *lstat;
     u32 *lhist, *ltile, *segagg;
     u32 *lbase;  // round 0: per block and digit slot, the pass's first position of every digit
@@ -987,7 +987,7 @@ __device__ __forceinline__ void cswap(u32 &ka, u32 &va, u32 &kb, u32 &vb) {
 }
 #define KGB_CS(i, j) cswap(k[i], v[i], k[j], v[j])
 
-__global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
+__global__ void __launch_bounds__(TPB, 4) k_group_thread(FwdArgs a) {
     const Ctl *ctl = a.ctl;
     const u32 rpar = ctl->rpar, h = ctl->h;
     // in and out share the id array: a group's ids stay in its slots; only descriptors move to the next list
@@ -1002,11 +1002,18 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
     u32 *isa_nxt = a.isa[rpar ^ 1];
     u32 *ids = in.eid;
     const u32 lane = lane_id();
-    for (u32 base = blockIdx.x * TPB; base < nseg; base += gridDim.x * TPB) {
+    const u32 stride = gridDim.x * TPB;
+    // software pipeline over the thread's groups: the next group's descriptor is loaded when this one starts, and
+    // its ids once this group's keys are in flight
+    Seg gq = {0, 0, 0, 0};
+    u32 vq[GTINY];
+    if (blockIdx.x * TPB + threadIdx.x < nseg) gq = in.seg[blockIdx.x * TPB + threadIdx.x];
+    for (u32 base = blockIdx.x * TPB; base < nseg; base += stride) {
         const u32 s = base + threadIdx.x;
         const bool ok = s < nseg;
         Seg g = {0, 0, 0, 0};
-        if (ok) g = in.seg[s];
+        if (ok) g = gq;
+        if (s + stride < nseg) gq = in.seg[s + stride];
         u32 len = g.len;
         if (len > GTINY || (u64)g.start + len > nslots) {  // broken list invariant: report, never overrun
             atomicOr(&a.ctl->err, E_SEG);
@@ -1016,7 +1023,7 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
         const u64 end = len ? blk_end(a, b) : 0;
         u32 k[GTINY], v[GTINY];
 #pragma unroll
-        for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? ids[g.start + q] : 0u;
+        for (u32 q = 0; q < GTINY; q++) v[q] = q < len ? (base == blockIdx.x * TPB ? ids[g.start + q] : vq[q]) : 0u;
         // In a round that follows repeat chains, a group whose chain is at least h long would come out of doubling
         // whole (its members' positions + h share one group); its chain key, the rank d + 1 positions on, orders it
         // at least as far, so it takes that key instead (one gather per member either way). Shorter chains, and
@@ -1027,6 +1034,11 @@ __global__ void __launch_bounds__(TPB) k_group_thread(FwdArgs a) {
 #pragma unroll
         for (u32 q = 0; q < GTINY; q++)
             k[q] = q >= len ? 0xFFFFFFFFu : by_chain ? chain_key(isa_cur, v[q], d, end) : rank_key(isa_cur, v[q], h, end);
+        {
+            const u32 lq = gq.len <= GTINY && (u64)gq.start + gq.len <= nslots && s + stride < nseg ? gq.len : 0u;
+#pragma unroll
+            for (u32 q = 0; q < GTINY; q++) vq[q] = q < lq ? ids[gq.start + q] : 0u;
+        }
         const u32 mlen = __reduce_max_sync(0xffffffffu, len);
         if (mlen <= 2) {
             KGB_CS(0, 1);
@@ -1821,10 +1833,10 @@ void FwdEngine::layout(u64 ncap, u32 bcap, u32 icap, bool want_sa, Add add) {
     add((void **)&d_orand, nseg_large * 8);
     add((void **)&d_orand64, nseg_large * 16);
     const u64 ltiles = n / LSD_TILE + bcap + 2, stiles = n / SEG_TILE + 2;
-    // the round-0 radix buffers (ids, ping-pong) alias the bucket-pass work lists K0 / K1, and the key groups alias
-    // the large list L0 and the keyed small list KS: round 0 on the LSD path uses none of those lists,
-    // and in the rank rounds the medium-key scratch (lval[0]) is written after the round's bucket passes and read
-    // before the next round's
+    // the round-0 radix items (8 bytes each, ping-pong) alias the bucket-pass work lists: item buffer q spans K_q's
+    // id array and the key array laid out right after it (checked in grow()). Round 0 on the LSD path uses neither
+    // list, and in the rank rounds the medium-key scratch (lval[0]) is written after the round's bucket passes and
+    // read before the next round's
     add((void **)&d_lstat, ltiles * 256 * 8);
     add((void **)&d_segbits, n / 8 + 64);
     add((void **)&d_lhist, (size_t)bcap * 256 * 4);  // byte histogram of every block
@@ -1883,8 +1895,11 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     for (auto &it : items) { *it.p = (char *)pool + off; off += it.bytes; }
     lists[L_P1].eid = lists[L_P0].eid;
     lists[L_L1].ekey = lists[L_L0].ekey;
-    d_lval[0] = lists[L_K0].eid; d_lval[1] = lists[L_K0].ekey;
-    d_lhi[0] = lists[L_K1].eid; d_lhi[1] = lists[L_K1].ekey;
+    d_lval[0] = lists[L_K0].eid; d_lval[1] = lists[L_K1].eid;
+    d_lhi[0] = lists[L_K0].ekey; d_lhi[1] = lists[L_K1].ekey;
+    for (int q = 0; q < 2; q++)  // round 0's 8-byte items need each id array and its key array to be adjacent
+        if ((char *)d_lhi[q] != (char *)d_lval[q] + align_up(std::max<size_t>(n * 4, 16), 256))
+            return record_cuda_error(cudaErrorInvalidValue, "forward workspace layout", __FILE__, __LINE__);
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemset(lists[l].tbig, 0xFF, ntm_small * 4));
     // orand rows start as (or = 0, and = ~0)
@@ -1912,7 +1927,7 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
 void FwdEngine::set_caps(FwdArgs &a) const {
     a.orand64 = d_orand64;
     for (int q = 0; q < 2; q++) { a.lval[q] = d_lval[q]; a.lhi[q] = d_lhi[q]; }
-    a.lkey[0] = lists[L_L0].eid; a.lkey[1] = lists[L_KS].eid;
+    for (int q = 0; q < 2; q++) a.lit[q] = reinterpret_cast<unsigned long long *>(d_lval[q]);
     a.segbits = d_segbits;
     a.lstat = d_lstat; a.lhist = d_lhist; a.ltile = d_ltile; a.segagg = d_segagg; a.lbase = d_lbase;
     a.cbits = d_cbits; a.cnz = d_cnz; a.ctn = d_ctn;

@@ -170,8 +170,7 @@ __global__ void __launch_bounds__(TPB) k_lsd_ident(FwdArgs a) {
 }
 
 struct LsdSmem {
-    u32 val[LSD_TILE];
-    u32 key[LSD_TILE];
+    unsigned long long item[LSD_TILE];
     u16 wcnt[TPB / 32][256];
     u32 gbase[256];
     u32 ws[TPB / 32 + 1];
@@ -202,7 +201,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     const bool head = tile == __ldg(&a.blk[tl.b].lt0);  // the block's first tile: its counts are the inclusive prefix
     // this pass's first position of digit tid in the block
     const u32 dbase = __ldg(a.lbase + ((u64)tl.b * NSLOT + slot) * 256 + tid);
-    const u32 *vin = a.lval[par], *kin = a.lkey[par];
+    const unsigned long long *iin = a.lit[par];
     // rr: each item's rank in its warp's digit bucket (< 512), two 16-bit ranks per register; the digit itself is
     // recomputed from the key where it is needed
     u32 v[LSD_IPT], rr[LSD_IPT / 2], k[LSD_IPT];
@@ -224,8 +223,9 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         for (int j = 0; j < LSD_IPT; j++) {
             const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
             const bool ok = x < cnt;
-            v[j] = ok ? __ldcs(vin + base + x) : 0u;
-            k[j] = ok ? __ldcs(kin + base + x) : 0u;
+            const unsigned long long it = ok ? __ldcs(iin + base + x) : 0ull;
+            v[j] = (u32)it;
+            k[j] = (u32)(it >> 32);
         }
     }
 #pragma unroll
@@ -262,8 +262,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         if (x < cnt) {
             const u32 d = (k[j] >> dsh) & 0xFFu;
             const u32 p = S.wcnt[warp][d] + ((rr[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
-            S.val[p] = v[j];
-            S.key[p] = k[j];
+            S.item[p] = (unsigned long long)k[j] << 32 | v[j];
         }
     }
     u32 excl = 0;
@@ -303,7 +302,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     }
     S.gbase[tid] = dbase + excl - dstart;
     __syncthreads();
-    u32 *vout = a.lval[par ^ 1], *kout = a.lkey[par ^ 1];
+    unsigned long long *iout = a.lit[par ^ 1];
     const BlockInfo bi = a.blk[tl.b];
     const u32 bend = bi.soff + bi.n;  // bound of the checked build's write checks
     (void)bend;
@@ -312,11 +311,9 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
     const int gn = higher ? (int)lsd_slot_group(__ffs(higher) - 1) : -1;
     if (gn == (int)g) {
         for (u32 i = tid; i < cnt; i += TPB) {
-            const u32 dst = S.gbase[(S.key[i] >> dsh) & 0xFFu] + i;
-            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) {
-                __stcs(vout + dst, S.val[i]);
-                __stcs(kout + dst, S.key[i]);
-            }
+            const unsigned long long it = S.item[i];
+            const u32 dst = S.gbase[((u32)(it >> 32) >> dsh) & 0xFFu] + i;
+            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(iout + dst, it);
         }
     } else if (gn >= 0) {
         const u64 end = (u64)bi.off + bi.n;
@@ -327,22 +324,24 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
             for (int q = 0; q < WB; q++) {
                 const u32 i = i0 + q * TPB;
                 const bool ok = i < cnt;
-                id[q] = ok ? S.val[i] : 0u;
-                dst[q] = ok ? S.gbase[(S.key[i] >> dsh) & 0xFFu] + i : 0u;
+                const unsigned long long it = ok ? S.item[i] : 0ull;
+                id[q] = (u32)it;
+                dst[q] = ok ? S.gbase[((u32)(it >> 32) >> dsh) & 0xFFu] + i : 0u;
                 kk[q] = ok ? lsd_group(a.T, id[q], (u32)gn, end) : 0u;
             }
 #pragma unroll
             for (int q = 0; q < WB; q++) {
                 if (i0 + q * TPB < cnt && KGB_OK(dst[q] < bend, &a.ctl->err, E_LIST)) {
-                    __stcs(vout + dst[q], id[q]);
-                    __stcs(kout + dst[q], kk[q]);
+                    __stcs(iout + dst[q], (unsigned long long)kk[q] << 32 | id[q]);
                 }
             }
         }
     } else {  // the last pass: the segmentation reads ids only
+        u32 *vout = a.lval[par ^ 1];
         for (u32 i = tid; i < cnt; i += TPB) {
-            const u32 dst = S.gbase[(S.key[i] >> dsh) & 0xFFu] + i;
-            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(vout + dst, S.val[i]);
+            const unsigned long long it = S.item[i];
+            const u32 dst = S.gbase[((u32)(it >> 32) >> dsh) & 0xFFu] + i;
+            if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(vout + dst, (u32)it);
         }
     }
 }
@@ -367,7 +366,7 @@ __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
     v.val = a.lval[par];
     v.bits = a.segbits;
     v.gbase = a.lval[par ^ 1];
-    v.gidx = a.lhi[par ^ 1];
+    v.gidx = a.lhi[par ^ 1];  // lval[q] and lhi[q] are the two halves of item buffer q
     v.m = c->m;
     return v;
 }
