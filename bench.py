@@ -855,6 +855,43 @@ def run_reference(args, world, rank):
             "e2e": {"value": round(v, 2), "unit": "MiB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def probe_random():
+    """Random 4-byte access rates of this GPU against the size of the array they hit: 64 M independent gathers
+    (torch index_select with int32 indices) and scatters (index_copy_ with int64 indices), CUDA events, best of four.
+    The rates include each call's sequential index read and, for gathers, its output write. They are the ceiling of a
+    kernel whose loads are random and independent: the inverse walk's psi loads and the rank rounds' rank gathers
+    hit arrays of 4 bytes per text byte (256 MiB for a 64 MiB block)."""
+    import torch
+
+    nops = 64 << 20
+    g = torch.Generator(device="cuda")
+    out = []
+    for mib in (64, 128, 256, 1024, 4096):
+        n = (mib << 20) // 4
+        arr = torch.ones(n, dtype=torch.int32, device="cuda")
+        g.manual_seed(mib)
+        idx = torch.randint(0, n, (nops,), device="cuda", dtype=torch.int64, generator=g)
+        idx32 = idx.to(torch.int32)
+        src = torch.zeros(nops, dtype=torch.int32, device="cuda")
+
+        def best(fn):
+            t = []
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                torch.cuda.synchronize()
+                t.append(e0.elapsed_time(e1))
+            return min(t[1:])
+        tg = best(lambda: torch.index_select(arr, 0, idx32))
+        ts = best(lambda: arr.index_copy_(0, idx, src))
+        out.append({"array_mib": mib, "gathers_G_per_s": round(nops / tg / 1e6, 1),
+                    "scatters_G_per_s": round(nops / ts / 1e6, 1)})
+        del arr, idx, idx32, src
+    return {"probe": "random_4byte_access", "ops": nops, "device": torch.cuda.get_device_name(), "results": out}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -880,7 +917,12 @@ def main():
                     help="time the plain path (one launch per kernel, host sync per round) instead of the graph")
     ap.add_argument("--skip-extras", action="store_true",
                     help="timed steps only: no e2e, profiled pass or CPU baseline (for profiler captures)")
+    ap.add_argument("--probe-random", action="store_true",
+                    help="print this GPU's random 4-byte gather and scatter rates by array size, and exit")
     args = ap.parse_args()
+    if args.probe_random:
+        print(json.dumps(probe_random()), flush=True)
+        return
     world, rank, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, world, rank)
