@@ -177,27 +177,17 @@ struct LsdSmem {
     u32 tile;
 };
 
-// One LSD pass over digit `slot` (skipped when that key byte is constant within every block): rank the tile's
-// suffixes by digit, publish the tile's digit counts, look back over the block's earlier tiles for the offsets
-// (bounded spin), stage the tile in shared memory in digit order and write it out in runs.
-__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
-    const Ctl *c = a.ctl;
-    const u32 act = active_slots(c);
-    if (!((act >> slot) & 1)) return;
+// One sort tile of an LSD pass over digit `slot`: rank the tile's suffixes by digit, publish the tile's digit counts,
+// look back over the block's earlier tiles for the offsets (bounded spin), stage the tile in shared memory in digit
+// order and write it out in runs. FULL: the tile holds LSD_TILE suffixes (every tile but a block's last), so no
+// element needs a bounds check.
+template <bool FULL>
+__device__ __forceinline__ void lsd_pass_tile(const FwdArgs &a, LsdSmem &S, int slot, u32 act, u64 epoch, u32 tile,
+                                              const LsdTile &tl) {
     const u32 lower = act & ((1u << slot) - 1), higher = act & ~((2u << slot) - 1);
     const u32 par = __popc(lower) & 1;
-    const u32 ntiles = c->lsd_tiles;
-    const u64 epoch = (u64)((c->seq << 5) | (u32)slot) << 32;
     const u32 tid = threadIdx.x, lane = lane_id(), warp = warp_id();
-    if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
-    for (int i = tid; i < (TPB / 32) * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
-    __syncthreads();
-    const u32 tile = S.tile;
-    if (tile >= ntiles) return;
-    const LsdTile tl = lsd_tile(a, tile);
-    const u32 base = tl.base, cnt = tl.cnt;
+    const u32 base = tl.base, cnt = FULL ? (u32)LSD_TILE : tl.cnt;
     const bool head = tile == __ldg(&a.blk[tl.b].lt0);  // the block's first tile: its counts are the inclusive prefix
     // this pass's first position of digit tid in the block
     const u32 dbase = __ldg(a.lbase + ((u64)tl.b * NSLOT + slot) * 256 + tid);
@@ -216,13 +206,13 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
         for (int j = 0; j < LSD_IPT; j++) {
             const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
             v[j] = id0 + x;
-            k[j] = x < cnt ? lsd_group(a.T, id0 + x, g, end) : 0u;
+            k[j] = (FULL || x < cnt) ? lsd_group(a.T, id0 + x, g, end) : 0u;
         }
     } else {
 #pragma unroll
         for (int j = 0; j < LSD_IPT; j++) {
             const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-            const bool ok = x < cnt;
+            const bool ok = FULL || x < cnt;
             const unsigned long long it = ok ? __ldcs(iin + base + x) : 0ull;
             v[j] = (u32)it;
             k[j] = (u32)(it >> 32);
@@ -231,13 +221,13 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        const u32 d = x < cnt ? (k[j] >> dsh) & 0xFFu : 0x100u;  // 0x100: past the tile's end
+        const u32 d = (FULL || x < cnt) ? (k[j] >> dsh) & 0xFFu : 0x100u;  // 0x100: past the tile's end
         const u32 peers = __match_any_sync(0xffffffffu, d);
-        const u32 before = d < 256 ? S.wcnt[warp][d] : 0u;
+        const u32 before = (FULL || d < 256) ? S.wcnt[warp][d] : 0u;
         const u32 r = before + __popc(peers & lanemask_lt());
         if (j & 1) rr[j >> 1] |= r << 16; else rr[j >> 1] = r;
         __syncwarp();
-        if (d < 256 && (__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
+        if ((FULL || d < 256) && (__ffs(peers) - 1) == (int)lane) S.wcnt[warp][d] = (u16)(before + __popc(peers));
         __syncwarp();
     }
     __syncthreads();
@@ -259,7 +249,7 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
 #pragma unroll
     for (int j = 0; j < LSD_IPT; j++) {
         const u32 x = warp * (32 * LSD_IPT) + j * 32 + lane;
-        if (x < cnt) {
+        if (FULL || x < cnt) {
             const u32 d = (k[j] >> dsh) & 0xFFu;
             const u32 p = S.wcnt[warp][d] + ((rr[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
             S.item[p] = (unsigned long long)k[j] << 32 | v[j];
@@ -344,6 +334,27 @@ __global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
             if (KGB_OK(dst < bend, &a.ctl->err, E_LIST)) __stcs(vout + dst, (u32)it);
         }
     }
+}
+
+// One LSD pass over digit `slot` (skipped when that key byte is constant within every block): each CTA takes the
+// next sort tile in order.
+__global__ void __launch_bounds__(TPB, 3) k_lsd_pass(FwdArgs a, int slot) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LsdSmem &S = *reinterpret_cast<LsdSmem *>(smem_raw);
+    const Ctl *c = a.ctl;
+    const u32 act = active_slots(c);
+    if (!((act >> slot) & 1)) return;
+    const u32 ntiles = c->lsd_tiles;
+    const u64 epoch = (u64)((c->seq << 5) | (u32)slot) << 32;
+    const u32 tid = threadIdx.x;
+    if (tid == 0) S.tile = atomicAdd(&a.ltile[slot], 1u);
+    for (int i = tid; i < (TPB / 32) * 256; i += TPB) (&S.wcnt[0][0])[i] = 0;
+    __syncthreads();
+    const u32 tile = S.tile;
+    if (tile >= ntiles) return;
+    const LsdTile tl = lsd_tile(a, tile);
+    if (tl.cnt == (u32)LSD_TILE) lsd_pass_tile<true>(a, S, slot, act, epoch, tile, tl);
+    else lsd_pass_tile<false>(a, S, slot, act, epoch, tile, tl);
 }
 
 // ---- segmentation of the sorted keys
