@@ -368,6 +368,7 @@ struct SegBufs {
     const u32 *val;
     u32 *bits;          // start bitmask
     u32 *gbase, *gidx;  // per group start: list slot base, list index | GRP_LARGE (free value buffers)
+    u32 *rk;            // per position: the round-0 rank, for the rank passes (the free half of the ids' item buffer)
     u32 m;
 };
 __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
@@ -378,6 +379,7 @@ __device__ __forceinline__ SegBufs seg_bufs(const FwdArgs &a) {
     v.bits = a.segbits;
     v.gbase = a.lval[par ^ 1];
     v.gidx = a.lhi[par ^ 1];  // lval[q] and lhi[q] are the two halves of item buffer q
+    v.rk = a.lhi[par];
     v.m = c->m;
     return v;
 }
@@ -676,6 +678,10 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
                 seg_step(v, ch, j0 + q, carry, p, ok, st, en, gf);
                 pv[q] = p; gfv[q] = gf;
                 if (ok && !(st && en)) live |= 1u << q;  // groups of one were resolved by part 1
+                if (ok && a.rank_passes) {  // every position's rank, streamed by the rank passes
+                    const u32 b = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, p, ch.blo, ch.bhi);
+                    __stcg(v.rk + p, gf - a.blk[b].soff);
+                }
             }
             u32 idv[QB], giv[QB], gbv[QB];
 #pragma unroll
@@ -717,32 +723,32 @@ __global__ void __launch_bounds__(TPB) k_seg_emit2(FwdArgs a) {
 // Ranks after round 0 (every suffix: its group's first position in its block), for the suffixes whose id lies in
 // [lo, hi). The host runs one pass per id range of RANK_SPAN ids, so that the rank writes of a pass (a scatter over
 // 4 * RANK_SPAN bytes) stay in L2 and reach DRAM as whole sectors, instead of one read-modify-write per suffix;
-// every pass streams the sorted ids and the group-start bits again.
+// every pass streams the sorted ids again and reads the ranks that the second emit kernel wrote per position.
 constexpr u32 RANK_SPAN = 16u << 20;
 // More passes than this cost more streaming than the random writes they replace (about 4 ps per suffix and pass
 // against about 29 ps per random rank write, measured on a 64 MiB block): the emit kernels write the ranks instead,
 // as they do when no block exceeds RANK_SPAN suffixes (their writes then stay within one block's ids at a time).
 constexpr u32 RANK_PASSES_MAX = 4;
 __global__ void __launch_bounds__(TPB) k_seg_rank(FwdArgs a, u32 lo, u32 hi) {
-    __shared__ u32 wl[TPB / 32];
     Ctl *c = a.ctl;
     const SegBufs v = seg_bufs(a);
     u32 *isa_nxt = a.isa[c->rpar ^ 1];
-    const u32 ntiles = (v.m + SEG_TILE - 1) / SEG_TILE;
     const u32 span = hi - lo;
-    for (u32 t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const SegChunk ch = seg_chunk(a, v, t, wl);
-        u32 carry = ch.carry0;
-#pragma unroll 4
-        for (int j = 0; j < SEG_IPT; j++) {
-            u32 p, gf; bool ok, st, en;
-            seg_step(v, ch, j, carry, p, ok, st, en, gf);
-            if (!ok) continue;
-            const u32 id = __ldcs(v.val + p);
-            if (id - lo >= span) continue;
-            const u32 b = ch.blo == ch.bhi ? ch.blo : blk_of_pos(a, p, ch.blo, ch.bhi);
-            KGB_GUARD(id < a.cap_n, &c->err, E_RANK) isa_nxt[id] = gf - a.blk[b].soff;
+    // four positions per thread and step: one 16-byte load of their ids, the ranks loaded only where an id is in range
+    const u32 m4 = v.m / 4;
+    const uint4 *ids4 = reinterpret_cast<const uint4 *>(v.val);
+    for (u32 i = blockIdx.x * TPB + threadIdx.x; i < m4; i += gridDim.x * TPB) {
+        const uint4 q = __ldcs(ids4 + i);
+        const u32 id[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (id[k] - lo >= span) continue;
+            KGB_GUARD(id[k] < a.cap_n, &c->err, E_RANK) isa_nxt[id[k]] = __ldg(v.rk + 4 * i + k);
         }
-        __syncthreads();
+    }
+    for (u32 p = m4 * 4 + blockIdx.x * TPB + threadIdx.x; p < v.m; p += gridDim.x * TPB) {
+        const u32 id = v.val[p];
+        if (id - lo >= span) continue;
+        KGB_GUARD(id < a.cap_n, &c->err, E_RANK) isa_nxt[id] = v.rk[p];
     }
 }
