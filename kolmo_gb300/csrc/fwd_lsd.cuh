@@ -35,6 +35,27 @@ __device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u64 q, u64 end)
     if (rem < 8) k &= ~0ull << (8 * (8 - rem));
     return k;
 }
+// The zero-padded 16-byte prefix at position q as two big-endian words (k: bytes 0-7, k2: bytes 8-15, 0 past the
+// block end), from three aligned 8-byte loads; `two` false: k2 = 0 and only two loads. The text buffer holds 64 zero
+// bytes past its last block, so the third load stays inside it.
+__device__ __forceinline__ void lsd_key16(const u8 *__restrict__ T, u64 q, u64 end, bool two, u64 &k, u64 &k2) {
+    k = k2 = 0;
+    if (q >= end) return;
+    const u64 *p = reinterpret_cast<const u64 *>(T + (q & ~7ull));
+    const u64 a = __ldg(p), b = __ldg(p + 1), c = two ? __ldg(p + 2) : 0ull;
+    const u32 s = (u32)(q & 7) * 8;
+    const u64 w0 = s ? (a >> s) | (b << (64 - s)) : a, w1 = s ? (b >> s) | (c << (64 - s)) : b;
+    auto be = [](u64 w) {
+        return ((u64)__byte_perm((u32)w, 0, 0x0123) << 32) | (u64)__byte_perm((u32)(w >> 32), 0, 0x0123);
+    };
+    const u64 rem = end - q;
+    k = be(w0);
+    if (rem < 8) k &= ~0ull << (8 * (8 - rem));
+    if (two && rem > 8) {
+        k2 = be(w1);
+        if (rem < 16) k2 &= ~0ull << (8 * (16 - rem));
+    }
+}
 // Key group g (prefix bytes 4g..4g+3) of the suffix at id, big-endian, zero past the block end.
 __device__ __forceinline__ u32 lsd_group(const u8 *__restrict__ T, u32 id, u32 g, u64 end) {
     return (u32)(lsd_key(T, (u64)id + 4 * g, end) >> 32);
@@ -416,13 +437,13 @@ __global__ void __launch_bounds__(TPB) k_seg_count(FwdArgs a) {
             const u64 end = (u64)bi.off + bi.n;
             // the prefix's two 8-byte words (the second cut to its first W - 8 bytes), from the text
             const u32 id = ok ? v.val[p] : 0u;
-            u64 k = ok ? lsd_key(a.T, id, end) : 0ull;
-            u64 k2 = ok && two ? lsd_key(a.T, (u64)id + 8, end) & m2 : 0ull;
+            u64 k = 0, k2 = 0;
+            if (ok) lsd_key16(a.T, id, end, two, k, k2);
+            k2 &= m2;
             u64 kp = __shfl_up_sync(0xffffffffu, k, 1), k2p = __shfl_up_sync(0xffffffffu, k2, 1);
             if (lane == 0 && ok && p > bi.soff) {  // the neighbour is in the same block
-                const u32 idp = v.val[p - 1];
-                kp = lsd_key(a.T, idp, end);
-                k2p = two ? lsd_key(a.T, (u64)idp + 8, end) & m2 : 0ull;
+                lsd_key16(a.T, v.val[p - 1], end, two, kp, k2p);
+                k2p &= m2;
             }
             const bool st = ok && (p == bi.soff || k != kp || k2 != k2p);
             const u32 sb = __ballot_sync(0xffffffffu, st);
