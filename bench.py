@@ -169,7 +169,7 @@ def cpu_sorter(threads: int | None = None):
 
 
 def time_cpu(T: np.ndarray, r: int, budget_s: float, max_reps: int = 3, threads: int | None = None):
-    """fwd+inv MiB/s of the CPU sorter on T (repeated while the budget allows)."""
+    """fwd+inv MiB/s of the CPU sorter on T (repeated while the time limit budget_s allows)."""
     kind, fwd, inv, threads = cpu_sorter(threads)
     reps, total = 0, 0.0
     while reps < max_reps:

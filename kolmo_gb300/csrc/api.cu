@@ -160,7 +160,7 @@ int run_fwd_jobs(Worker &C, kgbwt_fwd_job *jobs, int32_t count, uint32_t flags) 
     if ((rc = E.run(s, !(flags & KGBWT_PLAIN)))) return fail(rc);
     // sampled indexes first (small); then each block's L column without its sentinel row: straight into the
     // caller's U when every U is page-locked (two device-to-host copies per block), else through one copy into pinned
-    // staging and host copies (device-to-host copies into pageable memory are staged by the driver, block by block)
+    // staging and host copies (device-to-host copies into pageable memory are staged by the CUDA driver, block by block)
     bool direct = true;
     for (size_t k = 0; k < dev.size() && direct; k++) direct = page_locked(jobs[dev[k]].U);
     if (!direct) {
