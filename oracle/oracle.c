@@ -1,4 +1,4 @@
-/* ORACLE -- test infrastructure only. This file is the CPU checker for the GPU BWT path; it is never part of the
+/* ORACLE -- test infrastructure only. This file is the CPU oracle of the GPU BWT path; it is never part of the
  * product. Only the tests, the smoke check and the benchmark's CPU-baseline leg load it.
  *
  * A plain-C restatement of the reference's block-sorting entry points (src/algo/sais/sais.c:12027-12082 of

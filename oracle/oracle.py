@@ -1,4 +1,4 @@
-"""ORACLE -- test infrastructure only: ctypes bindings for the CPU checker of the GPU BWT path.
+"""ORACLE -- test infrastructure only: ctypes bindings for the CPU oracle of the GPU BWT path.
 
 Two libraries live here, both built by ``oracle/Makefile``:
 

@@ -1,7 +1,7 @@
 """ORACLE -- test infrastructure only: stages the reference's own sources for machines without the reference tree.
 
 The GPU host has no copy of adnaneben/kolmo, and binaries built on this x86 container do not run on its Arm cores.
-This script copies the parts of the reference tree that the CPU checkers need into ``baseline/_ref/kolmo/`` (listed
+This script copies the parts of the reference tree that the CPU oracle needs into ``baseline/_ref/kolmo/`` (listed
 in ``.gitignore``: never committed, but carried with the working tree to the GPU host), where ``oracle/Makefile``
 compiles them:
 
