@@ -117,6 +117,13 @@ int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg);
  * table, 0 for the defaults. */
 int32_t kgbwt_tuning_load(const char *path);
 int32_t kgbwt_tuning_lookup(uint64_t n, int32_t *cfg);
+/* The same two reports with every configuration field: the first ncfg (1..KGBWT_CONFIG_FIELDS) of tile_cap,
+ * tile_ctas, msd_ctas, small_group, warp_path, lsd_round0, lsd_bytes, chain_from (cfg[7]: the first rank round whose
+ * tiny groups may follow repeat chains, 0 for none). Return values as kgbwt_tuning_lookup and
+ * kgbwt_engine_last_config; -1 for ncfg < 1. */
+#define KGBWT_CONFIG_FIELDS 8
+int32_t kgbwt_tuning_lookup_n(uint64_t n, int32_t *cfg, int32_t ncfg);
+int32_t kgbwt_engine_last_config_n(kgbwt_engine *e, int32_t *cfg, int32_t ncfg);
 /* Forward: text blocks in dT (16 readable bytes past the last block). Results: dL receives each block's L column
  * with its sentinel row (n + 1 bytes at off + block index; row p0 holds no text byte), dI the sampled indexes at
  * iout (dI[iout] = primary index), dSA (may be NULL) the suffix array at off. */

@@ -179,15 +179,16 @@ class Engine:
 
     def last_config(self) -> dict:
         """The configuration the last forward call ran with (caller settings over the tuning table)."""
-        c = np.zeros(7, np.int32)
-        native.lib().kgbwt_engine_last_config(self.h, c.ctypes.data)
+        c = np.zeros(len(CONFIG_FIELDS), np.int32)
+        native.lib().kgbwt_engine_last_config_n(self.h, c.ctypes.data, len(CONFIG_FIELDS))
         return dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
 
     def workspace_bytes(self) -> int:
         return int(native.lib().kgbwt_engine_workspace_bytes(self.h))
 
 
-CONFIG_FIELDS = ("tile_cap", "tile_ctas", "msd_ctas", "small_group", "warp_path", "lsd_round0", "lsd_bytes")
+CONFIG_FIELDS = ("tile_cap", "tile_ctas", "msd_ctas", "small_group", "warp_path", "lsd_round0", "lsd_bytes",
+                 "chain_from")
 
 
 def tuning_load(path) -> int:
@@ -197,8 +198,8 @@ def tuning_load(path) -> int:
 
 def tuning_lookup(n: int):
     """(from_table, config) that a batch of n bytes would run with."""
-    c = np.zeros(7, np.int32)
-    t = int(native.lib().kgbwt_tuning_lookup(n, c.ctypes.data))
+    c = np.zeros(len(CONFIG_FIELDS), np.int32)
+    t = int(native.lib().kgbwt_tuning_lookup_n(n, c.ctypes.data, len(CONFIG_FIELDS)))
     return t == 1, dict(zip(CONFIG_FIELDS, (int(x) for x in c)))
 
 

@@ -730,6 +730,28 @@ int32_t kgbwt_engine_last_config(kgbwt_engine *e, int32_t *cfg) {
     return 0;
 }
 
+// The configuration fields in their reporting order, the first ncfg of them (at most KGBWT_CONFIG_FIELDS).
+static void config_fields(const FwdConfig &c, int32_t *cfg, int32_t ncfg) {
+    const int32_t f[KGBWT_CONFIG_FIELDS] = {c.tile_cap,   c.tile_ctas,  c.msd_ctas,  c.small_group,
+                                            c.warp_path,  c.lsd_round0, c.lsd_bytes, c.chain_from};
+    for (int32_t i = 0; i < ncfg && i < KGBWT_CONFIG_FIELDS; i++) cfg[i] = f[i];
+}
+
+int32_t kgbwt_tuning_lookup_n(uint64_t n, int32_t *cfg, int32_t ncfg) {
+    if (!cfg || ncfg < 1) return -1;
+    FwdConfig c;
+    const bool t = tuned_config(n, &c);
+    config_fields(c, cfg, ncfg);
+    return t ? 1 : 0;
+}
+
+int32_t kgbwt_engine_last_config_n(kgbwt_engine *e, int32_t *cfg, int32_t ncfg) {
+    if (!e || !cfg || ncfg < 1) return -1;
+    std::lock_guard<std::mutex> lock(e->mu);
+    config_fields(e->fwd.cfg, cfg, ncfg);
+    return 0;
+}
+
 int32_t kgbwt_dropin_stats(int64_t *out, int32_t cap) {
     if (!out || cap < 0) return -1;
     Context &C = ctx();

@@ -132,6 +132,10 @@ def lib():
     L.kgbwt_tuning_load.restype = _I32
     L.kgbwt_tuning_lookup.argtypes = [ctypes.c_uint64, _P]
     L.kgbwt_tuning_lookup.restype = _I32
+    L.kgbwt_tuning_lookup_n.argtypes = [ctypes.c_uint64, _P, _I32]
+    L.kgbwt_tuning_lookup_n.restype = _I32
+    L.kgbwt_engine_last_config_n.argtypes = [_P, _P, _I32]
+    L.kgbwt_engine_last_config_n.restype = _I32
     L.libcubwt_allocate_device_storage.argtypes = [_P, ctypes.c_int64]
     L.libcubwt_allocate_device_storage.restype = ctypes.c_int64
     L.libcubwt_free_device_storage.argtypes = [_P]
@@ -161,6 +165,7 @@ EXPORTS = (
     "kgbwt_unbwt_noalloc", "kgbwt_dropin_stats", "kgbwt_server_create", "kgbwt_server_destroy", "kgbwt_server_submit", "kgbwt_server_wait",
     "kgbwt_server_cancel", "kgbwt_server_stats_read", "kgbwt_server_inject_oom", "kgbwt_server_plan",
     "kgbwt_estimate_bytes", "kgbwt_engine_last_config", "kgbwt_tuning_load", "kgbwt_tuning_lookup",
+    "kgbwt_tuning_lookup_n", "kgbwt_engine_last_config_n",
     "libcubwt_allocate_device_storage", "libcubwt_free_device_storage", "libcubwt_bwt_aux", "libcubwt_bwt",
     "libcubwt_unbwt",
 )

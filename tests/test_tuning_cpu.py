@@ -59,7 +59,39 @@ def test_no_table_gives_defaults(restore_table):
     assert codec.tuning_load(None) == 0
     hit, c = codec.tuning_lookup(64 << 20)
     assert not hit and c == {"tile_cap": 4096, "tile_ctas": 2, "msd_ctas": 8, "small_group": 64, "warp_path": 1,
-                             "lsd_round0": 1, "lsd_bytes": 16}
+                             "lsd_round0": 1, "lsd_bytes": 16, "chain_from": 1}
+
+
+def test_chain_rounds_by_bucket(tmp_path, restore_table):
+    """The first repeat-chain round is a per-bucket field (0: none; a bucket without it keeps the default, 1); values
+    above 64 are refused."""
+    t = {"buckets": [{"max_bytes": 1 << 20, "chain_from": 0}, {"max_bytes": 1 << 22, "chain_from": 3},
+                     {"max_bytes": 1 << 30}]}
+    p = tmp_path / "c.json"
+    p.write_text(json.dumps(t))
+    assert codec.tuning_load(p) == 3
+    assert [codec.tuning_lookup(n)[1]["chain_from"] for n in (1000, 2 << 20, 8 << 20)] == [0, 3, 1]
+    p.write_text(json.dumps({"buckets": [{"max_bytes": 10, "chain_from": 99}]}))
+    assert codec.tuning_load(p) == -1
+
+
+def test_config_report_lengths(restore_table):
+    """The short report fills exactly its seven fields; the full one any prefix of the eight."""
+    import numpy as np
+
+    from kolmo_gb300 import native
+
+    codec.tuning_load(None)
+    c = np.full(9, -7, np.int32)
+    assert native.lib().kgbwt_tuning_lookup(1000, c.ctypes.data) == 0
+    assert list(c[7:]) == [-7, -7]
+    c = np.full(9, -7, np.int32)
+    assert native.lib().kgbwt_tuning_lookup_n(1000, c.ctypes.data, 3) == 0
+    assert list(c[:3]) == [4096, 2, 8] and list(c[3:]) == [-7] * 6
+    c = np.full(9, -7, np.int32)
+    assert native.lib().kgbwt_tuning_lookup_n(1000, c.ctypes.data, 9) == 0
+    assert c[7] == 1 and c[8] == -7
+    assert native.lib().kgbwt_tuning_lookup_n(1000, c.ctypes.data, 0) == -1
 
 
 def test_packaged_table_parses_if_present(restore_table):
