@@ -36,13 +36,14 @@ __device__ __forceinline__ u64 lsd_key(const u8 *__restrict__ T, u64 q, u64 end)
     return k;
 }
 // The zero-padded 16-byte prefix at position q as two big-endian words (k: bytes 0-7, k2: bytes 8-15, 0 past the
-// block end), from three aligned 8-byte loads; `two` false: k2 = 0 and only two loads. The text buffer holds 64 zero
-// bytes past its last block, so the third load stays inside it.
+// block end), from three aligned 8-byte loads; `two` false: k2 = 0 and only two loads. The third load is made only
+// when byte q + 8 lies in the block, so no load reaches more than 15 bytes past the block's end (the padding that
+// callers of the engine guarantee).
 __device__ __forceinline__ void lsd_key16(const u8 *__restrict__ T, u64 q, u64 end, bool two, u64 &k, u64 &k2) {
     k = k2 = 0;
     if (q >= end) return;
     const u64 *p = reinterpret_cast<const u64 *>(T + (q & ~7ull));
-    const u64 a = __ldg(p), b = __ldg(p + 1), c = two ? __ldg(p + 2) : 0ull;
+    const u64 a = __ldg(p), b = __ldg(p + 1), c = two && end - q > 8 ? __ldg(p + 2) : 0ull;
     const u32 s = (u32)(q & 7) * 8;
     const u64 w0 = s ? (a >> s) | (b << (64 - s)) : a, w1 = s ? (b >> s) | (c << (64 - s)) : b;
     auto be = [](u64 w) {
