@@ -1898,8 +1898,13 @@ int FwdEngine::grow(u64 ncap, u32 bcap, u32 icap, bool want_sa) {
     d_lval[0] = lists[L_K0].eid; d_lval[1] = lists[L_K1].eid;
     d_lhi[0] = lists[L_K0].ekey; d_lhi[1] = lists[L_K1].ekey;
     for (int q = 0; q < 2; q++)  // round 0's 8-byte items need each id array and its key array to be adjacent
-        if ((char *)d_lhi[q] != (char *)d_lval[q] + align_up(std::max<size_t>(n * 4, 16), 256))
+        if ((char *)d_lhi[q] != (char *)d_lval[q] + align_up(std::max<size_t>(n * 4, 16), 256)) {
+            cudaFree(pool);  // leave no half-made workspace behind: the next call lays it out again
+            pool = nullptr;
+            pool_bytes = 0;
+            Ncap = 0;
             return record_cuda_error(cudaErrorInvalidValue, "forward workspace layout", __FILE__, __LINE__);
+        }
     KGB_CHECK(cudaMemset(d_hist, 0, nseg_large * 256 * 4));
     for (int l : {(int)L_S0, (int)L_S1, (int)L_KS}) KGB_CHECK(cudaMemset(lists[l].tbig, 0xFF, ntm_small * 4));
     // orand rows start as (or = 0, and = ~0)
