@@ -97,16 +97,24 @@ def _time_config(texts, cfg, reps):
     return statistics.median(times), ref
 
 
+def candidate_grid(quick: bool = False) -> list:
+    """Every configuration the tuner times (the prefix width only varies on the LSD round 0); quick: the first four."""
+    keys = list(CANDIDATES)
+    grid = [dict(zip(keys, vals)) for vals in itertools.product(*(CANDIDATES[k] for k in keys))]
+    grid = [g for g in grid if g["lsd_round0"] or g["lsd_bytes"] == CANDIDATES["lsd_bytes"][0]]
+    return grid[:4] if quick else grid
+
+
+def default_config() -> dict:
+    """The library's defaults: each field's first candidate."""
+    return {k: v[0] for k, v in CANDIDATES.items()}
+
+
 def tune(reps: int = 3, quick: bool = False, log=print):
     import torch
 
-    keys = list(CANDIDATES)
-    grid = [dict(zip(keys, vals)) for vals in itertools.product(*(CANDIDATES[k] for k in keys))]
-    # the prefix width only matters on the LSD round 0
-    grid = [g for g in grid if g["lsd_round0"] or g["lsd_bytes"] == CANDIDATES["lsd_bytes"][0]]
-    if quick:
-        grid = grid[:4]
-    default = {k: v[0] for k, v in CANDIDATES.items()}
+    grid = candidate_grid(quick)
+    default = default_config()
     buckets = []
     for bi, (name, spec) in enumerate(BUCKETS if not quick else BUCKETS[:2]):
         texts = _batch(spec, 0x5EED + 97 * bi)

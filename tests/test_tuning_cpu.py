@@ -100,3 +100,20 @@ def test_packaged_table_parses_if_present(restore_table):
     with open(PKG_TABLE) as f:
         n = len(json.load(f)["buckets"])
     assert codec.tuning_load(PKG_TABLE) == n
+
+
+def test_autotune_grid(restore_table):
+    """The autotuner's candidate grid: every field the library's table accepts, the prefix width varied only on the
+    LSD round 0, and the defaults (each field's first candidate) among the candidates."""
+    from kolmo_gb300 import autotune
+
+    assert set(autotune.CANDIDATES) == set(codec.CONFIG_FIELDS) - {"tile_cap"}
+    grid = autotune.candidate_grid()
+    default = autotune.default_config()
+    assert default in grid
+    # the defaults the tuner assumes are the library's own (no table loaded)
+    codec.tuning_load(None)
+    lib_default = codec.tuning_lookup(1 << 20)[1]
+    assert all(lib_default[k] == v for k, v in default.items())
+    assert all(g["lsd_bytes"] == 16 for g in grid if not g["lsd_round0"])
+    assert len(grid) == len({tuple(sorted(g.items())) for g in grid})
